@@ -1,0 +1,73 @@
+// Shared helpers of libfbpgpu: status handling, launch checks, jet layout.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/fbpgpu.h"
+
+namespace fbp {
+
+// Thread-local message for fbp_last_error().
+void set_error(const char* fmt, ...);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define FBP_REQUIRE(cond, code, ...)      \
+    do {                                  \
+        if (!(cond)) {                    \
+            ::fbp::set_error(__VA_ARGS__); \
+            return (code);                \
+        }                                 \
+    } while (0)
+
+#define FBP_CUDA_CHECK(expr)                                                           \
+    do {                                                                               \
+        cudaError_t e_ = (expr);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            ::fbp::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), \
+                             __FILE__, __LINE__);                                      \
+            return FBP_ERR_CUDA;                                                       \
+        }                                                                              \
+    } while (0)
+
+#define FBP_LAUNCH_CHECK() FBP_CUDA_CHECK(cudaGetLastError())
+
+constexpr int kSM = 152;  // GB300 SM count (grid sizing hint; queried at run time too)
+
+int sm_count();
+
+__host__ __device__ constexpr int popc_const(int v) {
+    return v == 0 ? 0 : (v & 1) + popc_const(v >> 1);
+}
+
+// Jet layout: [u, d/dx_0..d/dx_{XD-1}, d2/dx_i^2 for each bit i of D2 ascending].
+__host__ __device__ constexpr int jet_size(int xd, int d2) { return 1 + xd + popc_const(d2); }
+
+// Index of the s-th set bit of mask among bits 0..7 (0 when there is none).
+__host__ __device__ constexpr int nth_bit(int mask, int s) {
+    int c = 0;
+    for (int d = 0; d < 8; ++d)
+        if ((mask >> d) & 1) {
+            if (c == s) return d;
+            ++c;
+        }
+    return 0;
+}
+
+// Compile-time table of the set bits of a mask (up to 3): DimsOf<M>::get(s) is
+// the s-th set bit, folded to a constant when s is a constant.
+template <int M>
+struct DimsOf {
+    static constexpr int d0 = nth_bit(M, 0), d1 = nth_bit(M, 1), d2 = nth_bit(M, 2);
+    __host__ __device__ static constexpr int get(int s) { return s == 0 ? d0 : (s == 1 ? d1 : d2); }
+};
+
+inline int jet_size_rt(int xd, int d2) {
+    int c = 0;
+    for (int i = 0; i < xd; ++i) c += (d2 >> i) & 1;
+    return 1 + xd + c;
+}
+
+}  // namespace fbp

@@ -1,0 +1,50 @@
+// Launch wrappers for one compiled network shape; included by the jet_inst_*.cu
+// translation units, each of which instantiates a group of shapes.
+#pragma once
+
+#include "jet.cuh"
+
+namespace fbp {
+
+template <int XD, int H1, int H2, int D2>
+int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, float* pair_out, int grid,
+                   cudaStream_t st) {
+    using C = Cfg<XD, H1, H2, D2>;
+    FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward: nparam %d != %d for this shape", net.nparam, C::P);
+    forward_pairs_kernel<C><<<grid, FWD_THREADS, 0, st>>>(net, x, pr, pair_out);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+template <int XD, int H1, int H2, int D2>
+int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, const float* slot_out,
+                   float* grad_part, int grid, cudaStream_t st) {
+    using C = Cfg<XD, H1, H2, D2>;
+    FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "adjoint: nparam %d != %d for this shape", net.nparam, C::P);
+    const size_t shm = sizeof(SAdj<C>);
+    static bool attr_set = false;
+    if (!attr_set) {
+        FBP_CUDA_CHECK(cudaFuncSetAttribute(adjoint_pairs_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        attr_set = true;
+    }
+    adjoint_pairs_kernel<C><<<grid, AdjT<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+// Tries one shape; returns 1 (not this shape) or the launch status.
+template <int XD, int H1, int H2, int D2>
+int try_shape(int mode, const fbp_net& net, const float* x, const fbp_pairs& pr, const float* slot_out, float* out,
+              int grid, cudaStream_t st) {
+    if (net.xd != XD || net.h1 != H1 || net.h2 != H2 || net.d2mask != D2) return 1;
+    if (mode == 0) return launch_forward<XD, H1, H2, D2>(net, x, pr, out, grid, st);
+    return launch_adjoint<XD, H1, H2, D2>(net, x, pr, slot_out, out, grid, st);
+}
+
+}  // namespace fbp
+
+#define FBP_TRY(XD, H1, H2, D2)                                                            \
+    {                                                                                      \
+        int r_ = fbp::try_shape<XD, H1, H2, D2>(mode, *net, x, *pr, slot_out, out, grid, st); \
+        if (r_ != 1) return r_;                                                            \
+    }

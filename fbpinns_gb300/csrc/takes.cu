@@ -1,0 +1,543 @@
+// Interaction lists ("takes"): point-in-box count/fill over a uniform cell
+// grid, prefix scans, compaction, the stable subdomain-major pair sort and the
+// work queue.  All integer work; results are bit-exact with the reference's
+// inside_points / get_inputs (fbpinns/decompositions_base.py:24-84,
+// fbpinns/trainers.py:332-419).
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace fbp {
+
+// ---------------------------------------------------------------------------
+// cell lookup (must match fbpinns_gb300/decompositions.py:build_cell_grid)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cell_coord(float v, double lo, double inv_h, int nc) {
+    const double t = __dmul_rn(__dsub_rn((double)v, lo), inv_h);
+    double f = floor(t);
+    if (!(f >= 0.0)) f = 0.0;  // also maps NaN to cell 0
+    if (f > (double)(nc - 1)) f = (double)(nc - 1);
+    return (int)f;
+}
+
+template <int XD>
+__device__ __forceinline__ int cell_of(const float* xp, const fbp_boxes& b) {
+    int c = cell_coord(xp[XD - 1], b.lo[XD - 1], b.inv_h[XD - 1], b.ncell[XD - 1]);
+#pragma unroll
+    for (int d = XD - 2; d >= 0; --d) c = c * b.ncell[d] + cell_coord(xp[d], b.lo[d], b.inv_h[d], b.ncell[d]);
+    return c;
+}
+
+template <int XD>
+__device__ __forceinline__ bool inside_box(const float* xp, const float* __restrict__ xmins,
+                                           const float* __restrict__ xmaxs, int j) {
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < XD; ++d) {
+        const float v = xp[d];
+        in = in && (v >= xmins[j * XD + d]) && (v <= xmaxs[j * XD + d]);
+    }
+    return in;
+}
+
+template <int XD>
+__global__ void inside_count_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b,
+                                    int32_t* __restrict__ pt_count, int32_t* __restrict__ pt_nlvl,
+                                    uint64_t* __restrict__ pt_lvl, int32_t* __restrict__ model_count) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        float xp[XD];
+#pragma unroll
+        for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
+        const int c = cell_of<XD>(xp, b);
+        const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
+        int cnt = 0;
+        uint64_t lvl = 0;
+        for (int e = e0; e < e1; ++e) {
+            const int j = b.cell_boxes[e];
+            if (b.select && !b.select[j]) continue;
+            if (inside_box<XD>(xp, b.xmins, b.xmaxs, j)) {
+                ++cnt;
+                lvl |= 1ull << (b.pou[j] & 63);
+                if (model_count) atomicAdd(&model_count[j], 1);
+            }
+        }
+        pt_count[p] = cnt;
+        if (pt_nlvl) pt_nlvl[p] = __popcll(lvl);
+        if (pt_lvl) pt_lvl[p] = lvl;
+    }
+}
+
+template <int XD>
+__global__ void inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b,
+                                   const int32_t* __restrict__ pt_off, const int32_t* __restrict__ np_off,
+                                   const uint64_t* __restrict__ pt_lvl, int32_t* __restrict__ n_take,
+                                   int32_t* __restrict__ m_take, int32_t* __restrict__ p_take,
+                                   int32_t* __restrict__ np_take, int64_t s_cap, int64_t u_cap,
+                                   int32_t* __restrict__ status) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        float xp[XD];
+#pragma unroll
+        for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
+        const int c = cell_of<XD>(xp, b);
+        const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
+        const uint64_t lvl = pt_lvl[p];
+        const int64_t base = pt_off[p];
+        const int64_t ubase = np_off[p];
+        int k = 0;
+        for (int e = e0; e < e1; ++e) {
+            const int j = b.cell_boxes[e];
+            if (b.select && !b.select[j]) continue;
+            if (inside_box<XD>(xp, b.xmins, b.xmaxs, j)) {
+                const int64_t o = base + k;
+                ++k;
+                if (o >= s_cap) {
+                    atomicOr(status, FBP_STATUS_PAIR_OVERFLOW);
+                    continue;
+                }
+                const int lv = b.pou[j] & 63;
+                const uint64_t below = lv ? (lvl & ((1ull << lv) - 1ull)) : 0ull;
+                n_take[o] = (int32_t)p;
+                m_take[o] = j;
+                p_take[o] = (int32_t)(ubase + __popcll(below));
+            }
+        }
+        // unique (point, level) slots in ascending level order
+        uint64_t bits = lvl;
+        int r = 0;
+        while (bits) {
+            const int64_t o = ubase + r;
+            if (o < u_cap)
+                np_take[o] = (int32_t)p;
+            else
+                atomicOr(status, FBP_STATUS_SLOT_OVERFLOW);
+            bits &= bits - 1ull;
+            ++r;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int32 (3 kernels, deterministic)
+// ---------------------------------------------------------------------------
+constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_TILE = SCAN_T * SCAN_V;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* smem_warp, int& total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) smem_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        int w = lane < nw ? smem_warp[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < nw) smem_warp[lane] = wi - w;
+        if (lane == nw - 1) smem_warp[32] = wi;
+    }
+    __syncthreads();
+    total = smem_warp[32];
+    const int r = incl - v + smem_warp[wid];
+    __syncthreads();
+    return r;
+}
+
+__global__ void scan_reduce_kernel(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ sums) {
+    __shared__ int sw[33];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int s = 0;
+#pragma unroll
+    for (int v = 0; v < SCAN_V; ++v) {
+        const int64_t i = base + (int64_t)v * SCAN_T + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    int tot;
+    block_exclusive_scan(s, sw, tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of the tile sums in place, total at sums[nb]
+__global__ void scan_sums_kernel(int32_t* __restrict__ sums, int64_t nb) {
+    __shared__ int sw[33];
+    int carry = 0;
+    for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+        const int64_t i = b0 + threadIdx.x;
+        const int v = i < nb ? sums[i] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, sw, tot);
+        if (i < nb) sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+__global__ void scan_down_kernel(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ sums,
+                                 int64_t nb, int32_t* __restrict__ out) {
+    __shared__ int sw[33];
+    __shared__ int tile[SCAN_TILE];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    // blocked arrangement: thread t owns items [t*V, t*V+V) of the tile
+#pragma unroll
+    for (int v = 0; v < SCAN_V; ++v) {
+        const int64_t i = base + (int64_t)v * SCAN_T + threadIdx.x;
+        tile[v * SCAN_T + threadIdx.x] = i < n ? in[i] : 0;
+    }
+    __syncthreads();
+    int loc[SCAN_V];
+    int s = 0;
+#pragma unroll
+    for (int v = 0; v < SCAN_V; ++v) {
+        loc[v] = s;
+        s += tile[threadIdx.x * SCAN_V + v];
+    }
+    int tot;
+    const int ex = block_exclusive_scan(s, sw, tot);
+    const int off = sums[blockIdx.x] + ex;
+#pragma unroll
+    for (int v = 0; v < SCAN_V; ++v) tile[threadIdx.x * SCAN_V + v] = off + loc[v];
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < SCAN_V; ++v) {
+        const int64_t i = base + (int64_t)v * SCAN_T + threadIdx.x;
+        if (i < n) out[i] = tile[v * SCAN_T + threadIdx.x];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[nb];
+}
+
+int scan_launch(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, cudaStream_t st) {
+    const int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 0) {
+        FBP_CUDA_CHECK(cudaMemsetAsync(out, 0, sizeof(int32_t), st));
+        return FBP_OK;
+    }
+    scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums);
+    FBP_LAUNCH_CHECK();
+    scan_sums_kernel<<<1, 1024, 0, st>>>(sums, nb);
+    FBP_LAUNCH_CHECK();
+    scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums, nb, out);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+size_t scan_scratch(int64_t n) { return (size_t)(((n + SCAN_TILE - 1) / SCAN_TILE) + 1) * sizeof(int32_t); }
+
+// ---------------------------------------------------------------------------
+// gather / compaction
+// ---------------------------------------------------------------------------
+__global__ void gather_i32_kernel(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ cnt,
+                                  const int32_t* __restrict__ inv, int32_t* __restrict__ out) {
+    const int64_t lim = cnt ? (int64_t)(*cnt) < n ? (int64_t)(*cnt) : n : n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < lim;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = inv[in[i]];
+}
+
+__global__ void flag_to_count_kernel(const int32_t* __restrict__ flag, int64_t n, int32_t* __restrict__ c) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        c[i] = flag[i] != 0;
+}
+
+__global__ void compact_kernel(const int32_t* __restrict__ flag, const int32_t* __restrict__ off, int64_t n,
+                               int32_t* __restrict__ out, int32_t* __restrict__ count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) out[off[i]] = (int32_t)i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = off[n];
+}
+
+// ---------------------------------------------------------------------------
+// Stable counting sort of pairs by subdomain.
+// Pass 1 (one warp per chunk of CH pairs): per-chunk histogram, written
+// bucket-major hist[j * nchunks + chunk].  Scan.  Pass 2: each warp re-reads
+// its chunk in order and scatters with ranks from __match_any_sync, keeping
+// per-bucket running counts in shared memory: stable and deterministic.
+// ---------------------------------------------------------------------------
+constexpr int SORT_CH = 4096;
+
+__global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ s_dev,
+                                 int64_t s_cap, int64_t m, int64_t nchunks, int32_t* __restrict__ hist) {
+    extern __shared__ int cnt[];
+    const int64_t s = min((int64_t)*s_dev, s_cap);
+    for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        for (int64_t j = threadIdx.x; j < m; j += blockDim.x) cnt[j] = 0;
+        __syncthreads();
+        const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
+        for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+            const int k = key[i];
+            if (k >= 0 && k < m) atomicAdd(&cnt[k], 1);
+        }
+        __syncthreads();
+        for (int64_t j = threadIdx.x; j < m; j += blockDim.x) hist[j * nchunks + ch] = cnt[j];
+        __syncthreads();
+    }
+}
+
+__global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
+                                    const int32_t* __restrict__ p_take, const int32_t* __restrict__ s_dev,
+                                    int64_t s_cap, int64_t m, int64_t nchunks,
+                                    const int32_t* __restrict__ hoff, int32_t* __restrict__ sd_pair,
+                                    int32_t* __restrict__ sd_point, int32_t* __restrict__ sd_slot) {
+    extern __shared__ int run[];  // per-bucket running offsets of this chunk
+    const int lane = threadIdx.x;  // blockDim.x == 32
+    const int64_t s = min((int64_t)*s_dev, s_cap);
+    for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        for (int64_t j = lane; j < m; j += 32) run[j] = hoff[j * nchunks + ch];
+        __syncwarp();
+        const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
+        for (int64_t i0 = b0; i0 < b1; i0 += 32) {
+            const int64_t i = i0 + lane;
+            const bool valid = i < b1;
+            int k = valid ? key[i] : -1;
+            if (valid && (k < 0 || k >= m)) k = -1;
+            const unsigned act = __ballot_sync(0xffffffffu, k >= 0);
+            const unsigned peers = __match_any_sync(0xffffffffu, k);
+            if (k >= 0) {
+                const unsigned lt = peers & ((1u << lane) - 1u);
+                const int leader = __ffs(peers) - 1;
+                const int base = run[k];
+                const int o = base + __popc(lt);
+                sd_pair[o] = (int32_t)i;
+                sd_point[o] = n_take[i];
+                sd_slot[o] = p_take[i];
+                __syncwarp(act);
+                if (lane == leader) run[k] = base + __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+}
+
+// sd_start[j] = hoff[j * nchunks] (start of bucket j), sd_start[m] = s
+__global__ void sort_starts_kernel(const int32_t* __restrict__ hoff, int64_t m, int64_t nchunks,
+                                   int32_t* __restrict__ sd_start) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j <= m;
+         j += (int64_t)gridDim.x * blockDim.x)
+        sd_start[j] = hoff[j * nchunks];
+}
+
+// ---------------------------------------------------------------------------
+// work queue
+// ---------------------------------------------------------------------------
+__global__ void work_count_kernel(const int32_t* __restrict__ sd_start, int64_t m, const uint8_t* __restrict__ sel,
+                                  int chunk, int32_t* __restrict__ nit) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = sd_start[j + 1] - sd_start[j];
+        nit[j] = (sel && !sel[j]) ? 0 : (c + chunk - 1) / chunk;
+    }
+}
+
+__global__ void work_fill_kernel(const int32_t* __restrict__ sd_start, int64_t m, const int32_t* __restrict__ ioff,
+                                 int chunk, int32_t* __restrict__ items, int32_t* __restrict__ item_start,
+                                 int32_t* __restrict__ n_items, int64_t cap, int32_t* __restrict__ status) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const int i0 = ioff[j], i1 = ioff[j + 1];
+        const int b = sd_start[j], e = sd_start[j + 1];
+        for (int it = i0; it < i1; ++it) {
+            if (it >= cap) {
+                atomicOr(status, FBP_STATUS_ITEM_OVERFLOW);
+                break;
+            }
+            const int beg = b + (it - i0) * chunk;
+            items[3 * (int64_t)it + 0] = (int32_t)j;
+            items[3 * (int64_t)it + 1] = beg;
+            items[3 * (int64_t)it + 2] = min(chunk, e - beg);
+        }
+        item_start[j] = min((int64_t)i0, cap);
+        if (j == m - 1) {
+            item_start[m] = min((int64_t)i1, cap);
+            *n_items = (int32_t)min((int64_t)i1, cap);
+        }
+    }
+}
+
+static int grid_for(int64_t n, int threads, int per_sm = 16) {
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+static int check_boxes(const fbp_boxes* b) {
+    FBP_REQUIRE(b, FBP_ERR_INVALID, "boxes: null");
+    FBP_REQUIRE(b->xd >= 1 && b->xd <= FBP_MAX_XD, FBP_ERR_UNSUPPORTED, "boxes: xd=%d not in 1..3", b->xd);
+    FBP_REQUIRE(b->xmins && b->xmaxs && b->pou && b->cell_start && b->cell_boxes, FBP_ERR_INVALID,
+                "boxes: null device pointer");
+    for (int d = 0; d < b->xd; ++d)
+        FBP_REQUIRE(b->ncell[d] >= 1, FBP_ERR_INVALID, "boxes: ncell[%d]=%d", d, b->ncell[d]);
+    return FBP_OK;
+}
+
+}  // namespace fbp
+
+using namespace fbp;
+
+extern "C" size_t fbp_scan_scratch_bytes(int64_t n) { return scan_scratch(n); }
+
+extern "C" int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch, size_t scratch_bytes,
+                            void* stream) {
+    FBP_REQUIRE(out && (in || n == 0), FBP_ERR_INVALID, "fbp_scan_i32: null pointer");
+    FBP_REQUIRE(n >= 0 && n < (int64_t)1 << 31, FBP_ERR_INVALID, "fbp_scan_i32: n=%lld", (long long)n);
+    FBP_REQUIRE(scratch && scratch_bytes >= scan_scratch(n), FBP_ERR_CAPACITY,
+                "fbp_scan_i32: scratch %zu < %zu", scratch_bytes, scan_scratch(n));
+    return scan_launch(in, out, n, (int32_t*)scratch, as_stream(stream));
+}
+
+extern "C" int fbp_inside_count(const float* x, int64_t n, const fbp_boxes* boxes, int32_t* pt_count,
+                                int32_t* pt_nlvl, uint64_t* pt_lvl, int32_t* model_count, void* stream) {
+    int rc = check_boxes(boxes);
+    if (rc) return rc;
+    FBP_REQUIRE(pt_count && (x || n == 0), FBP_ERR_INVALID, "fbp_inside_count: null pointer");
+    if (n == 0) return FBP_OK;
+    const int g = grid_for(n, 256);
+    cudaStream_t st = as_stream(stream);
+    switch (boxes->xd) {
+        case 1: inside_count_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
+        case 2: inside_count_kernel<2><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
+        case 3: inside_count_kernel<3><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
+    }
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+extern "C" int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes, const int32_t* pt_off,
+                               const int32_t* np_off, const uint64_t* pt_lvl, int32_t* n_take, int32_t* m_take,
+                               int32_t* p_take, int32_t* np_take, int64_t s_cap, int64_t u_cap, int32_t* status,
+                               void* stream) {
+    int rc = check_boxes(boxes);
+    if (rc) return rc;
+    FBP_REQUIRE(pt_off && np_off && pt_lvl && status && (x || n == 0), FBP_ERR_INVALID,
+                "fbp_inside_fill: null pointer");
+    FBP_REQUIRE((n_take && m_take && p_take) || s_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null take");
+    FBP_REQUIRE(np_take || u_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null np_take");
+    if (n == 0) return FBP_OK;
+    const int g = grid_for(n, 256);
+    cudaStream_t st = as_stream(stream);
+    switch (boxes->xd) {
+        case 1: inside_fill_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 2: inside_fill_kernel<2><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 3: inside_fill_kernel<3><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+    }
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+extern "C" int fbp_gather_i32(const int32_t* in, int64_t n, const int32_t* count_dev, const int32_t* inv,
+                              int32_t* out, void* stream) {
+    FBP_REQUIRE(inv && out && (in || n == 0), FBP_ERR_INVALID, "fbp_gather_i32: null pointer");
+    if (n == 0) return FBP_OK;
+    gather_i32_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(in, n, count_dev, inv, out);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+extern "C" size_t fbp_compact_scratch_bytes(int64_t n) {
+    return (size_t)(n + 1) * sizeof(int32_t) * 2 + scan_scratch(n) + 256;
+}
+
+extern "C" int fbp_compact_flags(const int32_t* flag, int64_t n, int32_t* out, int32_t* count_dev, void* scratch,
+                                 size_t scratch_bytes, void* stream) {
+    FBP_REQUIRE(out && count_dev && (flag || n == 0), FBP_ERR_INVALID, "fbp_compact_flags: null pointer");
+    FBP_REQUIRE(scratch && scratch_bytes >= fbp_compact_scratch_bytes(n), FBP_ERR_CAPACITY,
+                "fbp_compact_flags: scratch too small");
+    cudaStream_t st = as_stream(stream);
+    int32_t* c = (int32_t*)scratch;
+    int32_t* off = c + (n + 1);
+    int32_t* sums = off + (n + 1);
+    if (n == 0) {
+        FBP_CUDA_CHECK(cudaMemsetAsync(count_dev, 0, sizeof(int32_t), st));
+        return FBP_OK;
+    }
+    flag_to_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(flag, n, c);
+    FBP_LAUNCH_CHECK();
+    int rc = scan_launch(c, off, n, sums, st);
+    if (rc) return rc;
+    compact_kernel<<<grid_for(n, 256), 256, 0, st>>>(flag, off, n, out, count_dev);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+extern "C" size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m) {
+    const int64_t nch = (s_cap + SORT_CH - 1) / SORT_CH;
+    const int64_t hn = m * nch + 1;
+    return (size_t)hn * sizeof(int32_t) * 2 + scan_scratch(hn) + 256;
+}
+
+extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
+                              const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_pair,
+                              int32_t* sd_point, int32_t* sd_slot, void* scratch, size_t scratch_bytes,
+                              void* stream) {
+    FBP_REQUIRE(s_dev && sd_start && m > 0, FBP_ERR_INVALID, "fbp_sort_pairs: bad args");
+    FBP_REQUIRE(s_cap == 0 || (m_take && n_take && p_take && sd_pair && sd_point && sd_slot), FBP_ERR_INVALID,
+                "fbp_sort_pairs: null pointer");
+    FBP_REQUIRE(m * 4 <= 200 * 1024, FBP_ERR_UNSUPPORTED, "fbp_sort_pairs: m=%lld exceeds the shared-memory histogram",
+                (long long)m);
+    FBP_REQUIRE(scratch && scratch_bytes >= fbp_sort_scratch_bytes(s_cap, m), FBP_ERR_CAPACITY,
+                "fbp_sort_pairs: scratch too small");
+    cudaStream_t st = as_stream(stream);
+    const int64_t nch = (s_cap + SORT_CH - 1) / SORT_CH;
+    const int64_t hn = m * nch;
+    int32_t* hist = (int32_t*)scratch;
+    int32_t* hoff = hist + (hn + 1);
+    int32_t* sums = hoff + (hn + 1);
+    const size_t shm = (size_t)m * sizeof(int);
+    if (shm > 48 * 1024) {
+        FBP_CUDA_CHECK(cudaFuncSetAttribute(sort_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        FBP_CUDA_CHECK(cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    }
+    if (nch > 0) {
+        const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 8);
+        sort_hist_kernel<<<g, 256, shm, st>>>(m_take, s_dev, s_cap, m, nch, hist);
+        FBP_LAUNCH_CHECK();
+    }
+    int rc = scan_launch(hist, hoff, hn, sums, st);
+    if (rc) return rc;
+    if (nch > 0) {
+        const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32);
+        sort_scatter_kernel<<<g, 32, shm, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff, sd_pair,
+                                                 sd_point, sd_slot);
+        FBP_LAUNCH_CHECK();
+        sort_starts_kernel<<<grid_for(m + 1, 256), 256, 0, st>>>(hoff, m, nch, sd_start);
+        FBP_LAUNCH_CHECK();
+    } else {
+        FBP_CUDA_CHECK(cudaMemsetAsync(sd_start, 0, (size_t)(m + 1) * sizeof(int32_t), st));
+    }
+    return FBP_OK;
+}
+
+extern "C" size_t fbp_work_scratch_bytes(int64_t m) { return (size_t)(m + 1) * sizeof(int32_t) * 2 + scan_scratch(m) + 256; }
+
+extern "C" int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t* select, int32_t chunk,
+                              int32_t* items, int32_t* item_start, int32_t* n_items, int64_t items_cap,
+                              int32_t* status, void* scratch, size_t scratch_bytes, void* stream) {
+    FBP_REQUIRE(sd_start && items && item_start && n_items && status && m > 0 && chunk > 0, FBP_ERR_INVALID,
+                "fbp_build_work: bad args");
+    FBP_REQUIRE(scratch && scratch_bytes >= fbp_work_scratch_bytes(m), FBP_ERR_CAPACITY,
+                "fbp_build_work: scratch too small");
+    cudaStream_t st = as_stream(stream);
+    int32_t* nit = (int32_t*)scratch;
+    int32_t* ioff = nit + (m + 1);
+    int32_t* sums = ioff + (m + 1);
+    work_count_kernel<<<grid_for(m, 256), 256, 0, st>>>(sd_start, m, select, chunk, nit);
+    FBP_LAUNCH_CHECK();
+    int rc = scan_launch(nit, ioff, m, sums, st);
+    if (rc) return rc;
+    work_fill_kernel<<<grid_for(m, 256), 256, 0, st>>>(sd_start, m, ioff, chunk, items, item_start, n_items,
+                                                        items_cap, status);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}

@@ -1,0 +1,401 @@
+"""Device engine for the FBPINN training step.
+
+``FBPINNEngine`` owns the packed subdomain parameters (theta (m, P), the Adam
+moments, the shared step count) and launches the CUDA kernels of
+``libfbpgpu`` on point sets.  ``PointSet`` owns everything derived from one set
+of collocation points: the interaction lists, the subdomain-major pair order,
+the work queues and the per-pair / per-slot jet buffers.
+
+Step (fused path, built-in problems), all stream-ordered, no host sync:
+
+    forward_pairs   per-pair jets of u*w and w            (K-fwd)
+    pou_loss        POU combination, hard constraint, PDE residual,
+                    FP64 loss partials, per-slot seeds    (K-seg + K-loss)
+    loss_finalize   deterministic FP64 sum
+    adjoint_pairs   per-pair recompute + adjoint, one gradient partial per
+                    work item                             (K-adj)
+    grad_reduce     partials -> grad (m, P) in item order
+    adam            masked Adam with the shared count     (K-adam)
+
+With ``resample=True`` a step also draws new uniform points (Philox) and
+rebuilds the interaction lists on the device into fixed-capacity buffers, so
+the whole step can be captured in one CUDA graph.
+
+The generic path (any problem) uses ``FBPINNJet``: a torch.autograd.Function
+whose forward returns the per-point jets of the POU-combined network output
+and whose backward runs the adjoint kernels; ``constraining_fn`` and
+``loss_fn`` then run in torch autograd on the per-point jets only.
+"""
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .networks import fcn_param_count
+from .takes import PointTakes, grid_of
+
+
+def d2mask_of(required_ujss, xd):
+    """Bit mask of dims needing a pure second derivative; checks the orders.
+
+    Supports what the compiled jets carry: u, all first derivatives, and pure
+    second derivatives (the derivative tree of fbpinns/trainers.py:63-107
+    restricted to order <= 2 without mixed terms).
+    """
+    mask = 0
+    for req in required_ujss:
+        for iu, ixs in req:
+            if iu != 0:
+                raise NotImplementedError("only scalar solutions (ud=1) are compiled")
+            if len(ixs) > 2:
+                raise NotImplementedError(f"derivative order {len(ixs)} > 2 is not compiled")
+            if len(ixs) == 2:
+                if ixs[0] != ixs[1]:
+                    raise NotImplementedError(f"mixed derivative {ixs} is not compiled")
+                mask |= 1 << ixs[0]
+            for ix in ixs:
+                if not 0 <= ix < xd:
+                    raise ValueError(f"derivative index {ix} out of range for xd={xd}")
+    return mask
+
+
+def jet_index(xd, d2mask, ixs):
+    """Component of the jet layout holding d^len(ixs) u / dx_ixs."""
+    if len(ixs) == 0:
+        return 0
+    if len(ixs) == 1:
+        return 1 + ixs[0]
+    d = ixs[0]
+    return 1 + xd + bin(d2mask & ((1 << d) - 1)).count("1")
+
+
+def jet_size(xd, d2mask):
+    return 1 + xd + bin(d2mask).count("1")
+
+
+class PointSet:
+    """Interaction lists, subdomain-major pair order, work queues and jet buffers
+    of one set of points ``x`` (n, xd) on the device.
+
+    Sizes are either read back once (``caps=None``; like the reference's
+    ``s.item()``) or fixed capacities (``caps=(s_cap, u_cap)``), in which case
+    ``rebuild`` runs without any host synchronisation and overflow is
+    reported in ``status``.
+    """
+
+    def __init__(self, engine, x, select=None, caps=None, chunk=None):
+        self.eng = engine
+        g = engine.grid
+        self.n = int(x.shape[0])
+        self.x = x.to(g.device, torch.float32).contiguous()
+        self.J = engine.J
+        self.chunk = int(chunk or engine.chunk)
+        self.select = select
+        s_cap, u_cap = (None, None) if caps is None else caps
+        self.takes = PointTakes(g, self.n, s_cap=s_cap, u_cap=u_cap)
+        self.fixed_caps = caps is not None
+        self._sized = False
+        if caps is not None:
+            self._allocate(int(s_cap), int(u_cap))
+        self.rebuild()
+
+    # -- buffers -----------------------------------------------------------
+    def _allocate(self, s_cap, u_cap):
+        eng, dev, m = self.eng, self.eng.device, self.eng.m
+        self.s_cap, self.u_cap = s_cap, u_cap
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.sd_start = torch.zeros(m + 1, **i32)
+        self.sd_pair = torch.zeros(max(s_cap, 1), **i32)
+        self.sd_point = torch.zeros(max(s_cap, 1), **i32)
+        self.sd_slot = torch.zeros(max(s_cap, 1), **i32)
+        lib = _lib.load()
+        self.sort_scratch = torch.empty(int(lib.fbp_sort_scratch_bytes(s_cap, m)) // 4 + 1, **i32)
+        self.work_scratch = torch.empty(int(lib.fbp_work_scratch_bytes(m)) // 4 + 1, **i32)
+        self.items_cap = s_cap // self.chunk + m + 1
+        self.items_all = torch.zeros(3 * self.items_cap, **i32)
+        self.items_act = torch.zeros(3 * self.items_cap, **i32)
+        self.item_start_all = torch.zeros(m + 1, **i32)
+        self.item_start_act = torch.zeros(m + 1, **i32)
+        self.n_items_all = torch.zeros(1, **i32)
+        self.n_items_act = torch.zeros(1, **i32)
+        self.pair_out = torch.empty((max(s_cap, 1), 2 * self.J), dtype=torch.float32, device=dev)
+        self.slot_out = torch.empty((max(u_cap, 1), 2 * self.J), dtype=torch.float32, device=dev)
+        self.grad_part = torch.empty((self.items_cap, eng.P), dtype=torch.float32, device=dev)
+        self.U = torch.empty((self.n, self.J), dtype=torch.float32, device=dev)
+        self._sized = True
+
+    def rebuild(self, stream=None, state=None):
+        """(Re)build lists, sort and work queues for the current points and state."""
+        eng = self.eng
+        lib = _lib.load()
+        st = _lib.stream_ptr(stream)
+        sizes = self.takes.build(self.x, self.select, stream)
+        if sizes is not None:
+            s, u = sizes
+            if not self._sized or s > self.s_cap or u > self.u_cap:
+                self._allocate(s, u)
+            self.s, self.u = s, u
+        t = self.takes
+        _lib.check(lib.fbp_sort_pairs(_lib.ptr(t.m_take), _lib.ptr(t.n_take), _lib.ptr(t.p_take),
+                                      _lib.ptr(t.pt_off[self.n:]), self.s_cap, eng.m, _lib.ptr(self.sd_start),
+                                      _lib.ptr(self.sd_pair), _lib.ptr(self.sd_point), _lib.ptr(self.sd_slot),
+                                      _lib.ptr(self.sort_scratch), self.sort_scratch.numel() * 4, st),
+                   "fbp_sort_pairs")
+        self.build_work(stream, state)
+
+    def build_work(self, stream=None, state=None):
+        """Work queues: all subdomains with pairs (forward) and the active ones (adjoint)."""
+        eng = self.eng
+        lib = _lib.load()
+        st = _lib.stream_ptr(stream)
+        ws = self.work_scratch.numel() * 4
+        _lib.check(lib.fbp_build_work(_lib.ptr(self.sd_start), eng.m, None, self.chunk, _lib.ptr(self.items_all),
+                                      _lib.ptr(self.item_start_all), _lib.ptr(self.n_items_all), self.items_cap,
+                                      _lib.ptr(t_status(self)), _lib.ptr(self.work_scratch), ws, st),
+                   "fbp_build_work")
+        active = (eng.state == 1).to(torch.uint8) if state is None else state
+        self.adj_select = active.contiguous()
+        _lib.check(lib.fbp_build_work(_lib.ptr(self.sd_start), eng.m, _lib.ptr(self.adj_select), self.chunk,
+                                      _lib.ptr(self.items_act), _lib.ptr(self.item_start_act),
+                                      _lib.ptr(self.n_items_act), self.items_cap, _lib.ptr(t_status(self)),
+                                      _lib.ptr(self.work_scratch), ws, st), "fbp_build_work")
+
+    def pairs_struct(self, adjoint=False):
+        p = _lib.Pairs()
+        p.sd_start, p.sd_pair = _lib.ptr(self.sd_start), _lib.ptr(self.sd_pair)
+        p.sd_point, p.sd_slot = _lib.ptr(self.sd_point), _lib.ptr(self.sd_slot)
+        if adjoint:
+            p.items, p.n_items = _lib.ptr(self.items_act), _lib.ptr(self.n_items_act)
+        else:
+            p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
+        p.items_cap = self.items_cap
+        return p
+
+    def check_status(self):
+        self.takes.check_status()
+
+
+def t_status(ps):
+    return ps.takes.status
+
+
+class FBPINNEngine:
+    """Packed parameters + kernel launches for one decomposition and network shape."""
+
+    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None):
+        if not torch.cuda.is_available():
+            raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
+        _lib.load()
+        self.device = torch.device(device)
+        self.grid = grid_of(static_decomp, self.device)
+        self.m, self.xd = self.grid.m, self.grid.xd
+        ls = list(layer_sizes)
+        if ls[0] != self.xd:
+            raise ValueError(f"network input {ls[0]} != decomposition xd {self.xd}")
+        if ls[-1] != 1:
+            raise NotImplementedError("only scalar-output networks are compiled (ud=1)")
+        if len(ls) not in (3, 4):
+            raise NotImplementedError("the compiled FCN jets have one or two hidden layers")
+        self.layer_sizes = ls
+        self.h1 = ls[1]
+        self.h2 = ls[2] if len(ls) == 4 else 0
+        self.P = fcn_param_count(ls)
+        self.d2mask = int(d2mask)
+        self.J = jet_size(self.xd, self.d2mask)
+        self.chunk = int(chunk)
+        self.launch_grid = int(grid) if grid else 0
+        dev = self.device
+        self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
+        self.m1 = torch.zeros_like(self.theta)
+        self.m2 = torch.zeros_like(self.theta)
+        self.count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.state = torch.ones(self.m, dtype=torch.uint8, device=dev)
+        self.grad = torch.zeros_like(self.theta)
+        nparts = 8 * torch.cuda.get_device_properties(dev).multi_processor_count + 1
+        self.loss_part = torch.zeros(nparts, dtype=torch.float64, device=dev)
+        self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.npou = self.grid.npou
+        self._problem = None
+
+    # -- parameters ----------------------------------------------------------
+    def set_theta(self, theta):
+        self.theta.copy_(theta.to(self.device, torch.float32).reshape(self.m, self.P))
+
+    def set_state(self, active):
+        """active: (m,) ints, 0 = not trained, 1 = active, 2 = fixed (after get_inputs masking)."""
+        self.state.copy_(torch.as_tensor(np.asarray(active), dtype=torch.uint8).to(self.device))
+
+    def net_struct(self, theta=None, d2mask=None):
+        g = self.grid
+        n = _lib.Net()
+        n.xd, n.h1, n.h2, n.ud = self.xd, self.h1, self.h2, 1
+        n.d2mask = self.d2mask if d2mask is None else d2mask
+        n.nparam = self.P
+        n.theta = _lib.ptr(self.theta if theta is None else theta)
+        n.xmins, n.xmaxs, n.flags, n.unnorms = _lib.ptr(g.xmins), _lib.ptr(g.xmaxs), _lib.ptr(g.flags), _lib.ptr(g.unnorms)
+        n.m = self.m
+        return n
+
+    def set_problem(self, spec):
+        """Fused residual of a built-in problem (problems.Problem.fused_spec)."""
+        if spec is None:
+            self._problem = None
+            return
+        pr = _lib.Problem()
+        pr.kind = int(spec["kind"])
+        pr.n_int = int(spec.get("n_int", 0))
+        for i, v in enumerate(spec.get("p", [])):
+            pr.p[i] = float(v)
+        gauss = spec.get("gauss")
+        if gauss is not None:
+            self._gauss = torch.as_tensor(gauss, dtype=torch.float32).to(self.device).contiguous()
+            pr.gauss, pr.ng = _lib.ptr(self._gauss), int(self._gauss.shape[0])
+        else:
+            self._gauss = None
+            pr.gauss, pr.ng = None, 0
+        self._problem = pr
+
+    # -- kernels -------------------------------------------------------------
+    def points(self, x, select=None, caps=None, chunk=None):
+        return PointSet(self, x, select=select, caps=caps, chunk=chunk)
+
+    def forward_pairs(self, ps, theta=None, stream=None):
+        lib = _lib.load()
+        net = self.net_struct(theta)
+        pr = ps.pairs_struct(False)
+        _lib.check(lib.fbp_forward_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
+                                         self.launch_grid, _lib.stream_ptr(stream)), "fbp_forward_pairs")
+
+    def pou_forward(self, ps, stream=None):
+        lib = _lib.load()
+        t = ps.takes
+        _lib.check(lib.fbp_pou_forward(self.xd, self.d2mask, ps.n, self.npou, _lib.ptr(t.pt_off), _lib.ptr(t.p_take),
+                                       _lib.ptr(ps.pair_out), _lib.ptr(ps.slot_out), _lib.ptr(ps.U),
+                                       _lib.ptr(t.status), _lib.stream_ptr(stream)), "fbp_pou_forward")
+        return ps.U
+
+    def pou_backward(self, ps, Ubar, stream=None):
+        lib = _lib.load()
+        Ubar = Ubar.to(torch.float32).contiguous()
+        _lib.check(lib.fbp_pou_backward(self.xd, self.d2mask, ps.n, self.npou, _lib.ptr(ps.takes.np_off),
+                                        _lib.ptr(Ubar), _lib.ptr(ps.slot_out), _lib.stream_ptr(stream)),
+                   "fbp_pou_backward")
+
+    def pou_loss(self, ps, U_out=None, stream=None):
+        if self._problem is None:
+            raise RuntimeError("set_problem() first: the fused loss needs a built-in problem")
+        lib = _lib.load()
+        t = ps.takes
+        st = _lib.stream_ptr(stream)
+        _lib.check(lib.fbp_pou_loss(self.xd, self.d2mask, C.byref(self._problem), ps.n, self.npou, _lib.ptr(ps.x),
+                                    _lib.ptr(t.pt_off), _lib.ptr(t.np_off), _lib.ptr(t.p_take), _lib.ptr(ps.pair_out),
+                                    _lib.ptr(ps.slot_out), _lib.ptr(U_out), _lib.ptr(self.loss_part),
+                                    self.loss_part.numel(), _lib.ptr(t.status), st), "fbp_pou_loss")
+        _lib.check(lib.fbp_loss_finalize(_lib.ptr(self.loss_part), self.loss_part.numel(), 1.0 / ps.n,
+                                         _lib.ptr(self.loss), st), "fbp_loss_finalize")
+        return self.loss
+
+    def adjoint(self, ps, theta=None, out=None, stream=None):
+        lib = _lib.load()
+        st = _lib.stream_ptr(stream)
+        net = self.net_struct(theta)
+        pr = ps.pairs_struct(True)
+        _lib.check(lib.fbp_adjoint_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
+                                         _lib.ptr(ps.grad_part), self.launch_grid, st), "fbp_adjoint_pairs")
+        out = self.grad if out is None else out
+        _lib.check(lib.fbp_grad_reduce(_lib.ptr(ps.grad_part), _lib.ptr(ps.item_start_act), self.m, self.P,
+                                       _lib.ptr(out), st), "fbp_grad_reduce")
+        return out
+
+    def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8, eps_root=0.0, grad=None, stream=None):
+        lib = _lib.load()
+        g = self.grad if grad is None else grad
+        _lib.check(lib.fbp_adam(_lib.ptr(self.theta), _lib.ptr(self.m1), _lib.ptr(self.m2), _lib.ptr(g),
+                                _lib.ptr(self.state), self.m, self.P, lr, b1, b2, eps, eps_root,
+                                _lib.ptr(self.count), _lib.stream_ptr(stream)), "fbp_adam")
+
+    def fused_step(self, ps, lr, stream=None, **adam_kw):
+        """One training step on point set ps; returns the device loss (float64, 1 elem)."""
+        self.forward_pairs(ps, stream=stream)
+        loss = self.pou_loss(ps, stream=stream)
+        self.adjoint(ps, stream=stream)
+        self.adam(lr, stream=stream, **adam_kw)
+        return loss
+
+    def sample(self, x_out, seed, offset, xmin, xmax, stream=None):
+        lib = _lib.load()
+        lo = (C.c_double * 3)(*[float(v) for v in xmin])
+        hi = (C.c_double * 3)(*[float(v) for v in xmax])
+        _lib.check(lib.fbp_sample_uniform(_lib.ptr(x_out), x_out.shape[0], self.xd, lo, hi, seed, offset,
+                                          _lib.stream_ptr(stream)), "fbp_sample_uniform")
+
+
+class FBPINNJet(torch.autograd.Function):
+    """theta (m, P) -> per-point jets U (n, J) of the POU-combined network output.
+
+    forward: per-pair jet kernel + POU combination; backward: POU seeds +
+    per-pair adjoint kernel + gradient reduction.  Replaces the nested jvp of
+    ``FBPINN_model`` under ``value_and_grad`` (fbpinns/trainers.py:126-177,
+    197-247, 292) up to the constraining operator.
+    """
+
+    @staticmethod
+    def forward(ctx, theta, engine, ps):
+        theta = theta.contiguous()
+        engine.forward_pairs(ps, theta)
+        U = engine.pou_forward(ps).clone()
+        ctx.engine, ctx.ps = engine, ps
+        ctx.save_for_backward(theta)
+        return U
+
+    @staticmethod
+    def backward(ctx, Ubar):
+        (theta,) = ctx.saved_tensors
+        eng, ps = ctx.engine, ctx.ps
+        eng.pou_backward(ps, Ubar)
+        grad = torch.empty_like(theta)
+        eng.adjoint(ps, theta, out=grad)
+        return grad, None, None
+
+
+def constrained_jets(cfn, all_params, x, U, xd, d2mask):
+    """Jets of constraining_fn(all_params, x, u(x)) from the jets U of u.
+
+    For each dim d the Taylor model u(x + t e_d) = U0 + t U_d + t^2/2 U_dd is
+    pushed through cfn with nested forward-mode jvp in t (torch.func), which
+    gives d/dx_d and d^2/dx_d^2 of the constrained solution exactly, for any
+    constraining_fn; reverse mode through it is plain autograd.
+    """
+    n = x.shape[0]
+    J = U.shape[1]
+    out = [None] * J
+    u0 = U[:, 0:1]
+    out[0] = cfn(all_params, x, u0)
+    ones = torch.ones((n, 1), dtype=x.dtype, device=x.device)
+    zero = torch.zeros((n, 1), dtype=x.dtype, device=x.device)
+    for d in range(xd):
+        e = torch.zeros((1, xd), dtype=x.dtype, device=x.device)
+        e[0, d] = 1.0
+        ud = U[:, 1 + d:2 + d]
+        has2 = (d2mask >> d) & 1
+        if has2:
+            k = jet_index(xd, d2mask, (d, d))
+            udd = U[:, k:k + 1]
+
+            def h(t, ud=ud, udd=udd, e=e):
+                return cfn(all_params, x + t * e, u0 + t * ud + 0.5 * t * t * udd)
+
+            def g(t, h=h):
+                return torch.func.jvp(h, (t,), (ones,))[1]
+
+            d1, d2 = torch.func.jvp(g, (zero,), (ones,))
+            out[1 + d], out[k] = d1, d2
+        else:
+            def h(t, ud=ud, e=e):
+                return cfn(all_params, x + t * e, u0 + t * ud)
+
+            out[1 + d] = torch.func.jvp(h, (zero,), (ones,))[1]
+    return torch.cat(out, dim=1)

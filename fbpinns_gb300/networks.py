@@ -1,0 +1,175 @@
+"""Subdomain networks (the reference's ``fbpinns/networks.py`` API), in torch.
+
+``network_fn(params, x)`` evaluates one network on x (..., fan_in) — a single
+point or a batch; per-pair parameter batches (leading dim s) are supported by
+``batched_linear``.  Initialisation draws W, b ~ U(-1/sqrt(fan_in),
++1/sqrt(fan_in)) like ``FCN._random_layer_params`` (fbpinns/networks.py:51-58);
+the reference uses JAX's PRNG, this engine a seeded torch generator, so the
+draws differ but the distribution is the same.
+"""
+
+import math
+
+import torch
+
+
+def _gen(key):
+    if isinstance(key, torch.Generator):
+        return key
+    g = torch.Generator()
+    g.manual_seed(int(key))
+    return g
+
+
+def _uniform(g, shape, v):
+    return (torch.rand(shape, generator=g, dtype=torch.float64) * 2 - 1).mul_(v).float()
+
+
+def batched_linear(w, b, x):
+    """x @ w^T + b for w (..., fo, fi) and x (..., fi)."""
+    return torch.einsum("...ij,...j->...i", w, x) + b
+
+
+class Network:
+    """Base class (fbpinns/networks.py:14-34)."""
+
+    @staticmethod
+    def init_params(*args):
+        raise NotImplementedError
+
+    @staticmethod
+    def network_fn(params, x):
+        raise NotImplementedError
+
+
+class FCN(Network):
+    """tanh hidden layers, linear output (fbpinns/networks.py:39-68)."""
+
+    @staticmethod
+    def init_params(key, layer_sizes):
+        g = _gen(key)
+        layers = []
+        for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
+            v = math.sqrt(1.0 / fi)
+            layers.append((_uniform(g, (fo, fi), v), _uniform(g, (fo,), v)))
+        return {}, {"layers": layers}
+
+    @staticmethod
+    def network_fn(params, x):
+        layers = params["trainable"]["network"]["subdomain"]["layers"]
+        for w, b in layers[:-1]:
+            x = torch.tanh(batched_linear(w, b, x))
+        w, b = layers[-1]
+        return batched_linear(w, b, x)
+
+
+class AdaptiveFCN(Network):
+    """a tanh(x / a) activations (fbpinns/networks.py:70-100)."""
+
+    @staticmethod
+    def init_params(key, layer_sizes):
+        _, tp = FCN.init_params(key, layer_sizes)
+        return {}, {"layers": [(w, b, torch.ones_like(b)) for w, b in tp["layers"]]}
+
+    @staticmethod
+    def network_fn(params, x):
+        layers = params["trainable"]["network"]["subdomain"]["layers"]
+        for w, b, a in layers[:-1]:
+            x = a * torch.tanh(batched_linear(w, b, x) / a)
+        w, b, _ = layers[-1]
+        return batched_linear(w, b, x)
+
+
+class SIREN(Network):
+    """sin activations, U(+-sqrt(6/fan_in)) init (fbpinns/networks.py:102-131)."""
+
+    @staticmethod
+    def init_params(key, layer_sizes):
+        g = _gen(key)
+        layers = []
+        for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
+            v = math.sqrt(6.0 / fi)
+            layers.append((_uniform(g, (fo, fi), v), _uniform(g, (fo,), v)))
+        return {}, {"layers": layers}
+
+    @staticmethod
+    def network_fn(params, x):
+        layers = params["trainable"]["network"]["subdomain"]["layers"]
+        for w, b in layers[:-1]:
+            x = torch.sin(batched_linear(w, b, x))
+        w, b = layers[-1]
+        return batched_linear(w, b, x)
+
+
+class AdaptiveSIREN(Network):
+    """c sin(o x) activations (fbpinns/networks.py:133-163)."""
+
+    @staticmethod
+    def init_params(key, layer_sizes):
+        _, tp = SIREN.init_params(key, layer_sizes)
+        return {}, {"layers": [(w, b, torch.ones_like(b), torch.ones_like(b)) for w, b in tp["layers"]]}
+
+    @staticmethod
+    def network_fn(params, x):
+        layers = params["trainable"]["network"]["subdomain"]["layers"]
+        for w, b, c, o in layers[:-1]:
+            x = c * torch.sin(o * batched_linear(w, b, x))
+        w, b, _, _ = layers[-1]
+        return batched_linear(w, b, x)
+
+
+class FourierFCN(FCN):
+    """Fourier features [sin(omega x), cos(omega x)] then an FCN (fbpinns/networks.py:165-194)."""
+
+    @staticmethod
+    def init_params(key, layer_sizes, mu, sd, n_features):
+        g = _gen(key)
+        omega = (2 * math.pi * (mu + sd * torch.randn((n_features, layer_sizes[0]), generator=g,
+                                                      dtype=torch.float64))).float()
+        _, tp = FCN.init_params(g, [2 * n_features] + list(layer_sizes)[1:])
+        return {"omega": omega}, tp
+
+    @staticmethod
+    def network_fn(params, x):
+        omega = params["static"]["network"]["subdomain"]["omega"]
+        x = torch.einsum("...ij,...j->...i", omega, x)
+        x = torch.cat([torch.sin(x), torch.cos(x)], dim=-1)
+        return FCN.network_fn(params, x)
+
+
+def norm(mu, sd, x):
+    """fbpinns/networks.py:197-198."""
+    return (x - mu) / sd
+
+
+def unnorm(mu, sd, x):
+    """fbpinns/networks.py:200-201."""
+    return x * sd + mu
+
+
+# ---------------------------------------------------------------------------
+# packed parameter layout used by the CUDA kernels
+# ---------------------------------------------------------------------------
+
+def fcn_param_count(layer_sizes):
+    """P = sum over layers of fan_out * (fan_in + 1)."""
+    return sum(fo * (fi + 1) for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]))
+
+
+def pack_layers(layers):
+    """[(W (m,fo,fi), b (m,fo)), ...] -> theta (m, P): per layer W row-major then b."""
+    m = layers[0][0].shape[0]
+    return torch.cat([t.reshape(m, -1) for w, b in layers for t in (w, b)], dim=1).contiguous()
+
+
+def unpack_layers(theta, layer_sizes):
+    """theta (m, P) -> [(W, b), ...] as views into theta."""
+    out, o = [], 0
+    m = theta.shape[0]
+    for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
+        w = theta[:, o:o + fo * fi].view(m, fo, fi)
+        o += fo * fi
+        b = theta[:, o:o + fo]
+        o += fo
+        out.append((w, b))
+    return out

@@ -1,0 +1,274 @@
+/*
+ * fbpgpu.h — C ABI of the GB300 FBPINN training-step library (libfbpgpu.so).
+ *
+ * The library replaces, with hand-written sm_103a kernels, the device work of
+ * one FBPINN training step of the reference library (benmoseley/FBPINNs,
+ * fbpinns v0.2.0), i.e. what `FBPINN_update` (fbpinns/trainers.py:285-296)
+ * runs through XLA, plus the interaction-list construction that feeds it.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: FBP_OK (0) or a negative code;
+ *    fbp_last_error() gives a message for the calling thread.  No C++
+ *    exception crosses the ABI.
+ *  - All pointers are caller-owned DEVICE memory unless the parameter says
+ *    "host".  The library allocates nothing: scratch buffers are passed in
+ *    and their sizes are queried with the matching *_scratch_bytes function.
+ *  - Every call is stream-ordered on `stream` (a cudaStream_t, NULL = legacy
+ *    default stream) and never synchronises the host, so a sequence of calls
+ *    can be captured into a CUDA graph.  Data-dependent sizes (pair counts,
+ *    work items) stay on the device; kernels clamp to the capacities they are
+ *    given and report overflow through a device status word.
+ *  - Floating point is FP32; the loss is accumulated in FP64.  Indices are
+ *    int32, as in the reference (JAX without x64).
+ *
+ * Jet layout ("J components" per point or pair), for input dimension xd and a
+ * bit mask d2 of dimensions that need a pure second derivative:
+ *     [u, du/dx_0 .. du/dx_{xd-1}, d2u/dx_i^2 for each bit i of d2 (ascending)]
+ * J = 1 + xd + popcount(d2).  This is the per-point set of derivative jets
+ * that the reference obtains from nested forward-mode jvp
+ * (fbpinns/trainers.py:213-247, _get_ujs / jacfwd).
+ */
+#ifndef FBPGPU_H
+#define FBPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FBP_OK 0
+#define FBP_ERR_INVALID (-1)      /* bad argument (shape, size, pointer) */
+#define FBP_ERR_CUDA (-2)         /* a CUDA runtime call failed */
+#define FBP_ERR_UNSUPPORTED (-3)  /* configuration with no compiled kernel */
+#define FBP_ERR_CAPACITY (-4)     /* caller buffer too small */
+
+/* Device status word bits (written by kernels into an int32 the caller owns). */
+#define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */
+#define FBP_STATUS_SLOT_OVERFLOW 2      /* more (point, level) slots than capacity */
+#define FBP_STATUS_ITEM_OVERFLOW 4      /* more work items than capacity */
+#define FBP_STATUS_LEVEL_ORDER 8        /* a point's levels are not in ascending model order */
+#define FBP_STATUS_BAD_INDEX 16         /* an index out of range was skipped */
+
+/* Maximum compiled sizes. */
+#define FBP_MAX_XD 3
+#define FBP_MAX_LEVELS 64   /* distinct POU levels (bit mask per point) */
+
+/* ------------------------------------------------------------------ */
+/* Geometry of the subdomain boxes and the uniform cell grid that       */
+/* accelerates the point-in-box test.                                   */
+/* ------------------------------------------------------------------ */
+typedef struct fbp_boxes {
+    const float* xmins;        /* (m, xd) closed box lower corners */
+    const float* xmaxs;        /* (m, xd) upper corners */
+    const int32_t* pou;        /* (m,) POU level of each box, 0 <= pou < 64 */
+    const uint8_t* select;     /* (m,) nonzero = box takes part; NULL = all */
+    int64_t m;
+    int32_t xd;
+    /* cell grid: cell index along dim d of a coordinate v is
+     *   clamp(floor(((double)v - lo[d]) * inv_h[d]), 0, ncell[d]-1)
+     * computed with IEEE double round-to-nearest on host and device alike,
+     * so a box registered in cells [cell(xmin), cell(xmax)] is a candidate
+     * of every point it contains. */
+    int32_t ncell[FBP_MAX_XD];
+    double lo[FBP_MAX_XD];
+    double inv_h[FBP_MAX_XD];
+    const int32_t* cell_start;  /* (ncells+1,) CSR offsets, cell id = c0 + n0*(c1 + n1*c2) */
+    const int32_t* cell_boxes;  /* (entries,) box ids, ascending within each cell */
+} fbp_boxes;
+
+/* ------------------------------------------------------------------ */
+/* Network / decomposition description for the per-pair jet kernels.   */
+/* ------------------------------------------------------------------ */
+typedef struct fbp_net {
+    int32_t xd;           /* input dimension (1..3) */
+    int32_t h1;           /* first hidden width */
+    int32_t h2;           /* second hidden width (0 = one hidden layer) */
+    int32_t ud;           /* output dimension, must be 1 */
+    int32_t d2mask;       /* dims with a pure second-derivative jet */
+    int32_t nparam;       /* P: parameters per subdomain (packed layout below) */
+    /* theta (m, P): for each layer in order, W (fan_out, fan_in) row-major
+     * then b (fan_out) — the reference's FCN (w, b) list flattened
+     * (fbpinns/networks.py:43-68). */
+    const float* theta;
+    const float* xmins;   /* (m, xd) subdomain boxes (norm + window) */
+    const float* xmaxs;   /* (m, xd) */
+    const float* flags;   /* (m,) window flag (decompositions.py:169-172) */
+    const float* unnorms; /* (m, 2) (mu, sd) of the output unnormalisation */
+    int64_t m;
+} fbp_net;
+
+/* Pair lists sorted subdomain-major, and the work queue over them. */
+typedef struct fbp_pairs {
+    const int32_t* sd_start;  /* (m+1,) offsets of each subdomain's pairs */
+    const int32_t* sd_pair;   /* (s,) point-major pair index of each sorted pair */
+    const int32_t* sd_point;  /* (s,) point index of each sorted pair */
+    const int32_t* sd_slot;   /* (s,) (point, level) slot of each sorted pair */
+    const int32_t* items;     /* (cap, 3) work items: (subdomain, begin, count) */
+    const int32_t* n_items;   /* device count of valid items */
+    int64_t items_cap;
+} fbp_pairs;
+
+/* Built-in PDE residuals fused into the POU/loss kernel. */
+#define FBP_PROBLEM_NONE 0
+#define FBP_PROBLEM_HO_HARDBC 1     /* problems.py:149-206 */
+#define FBP_PROBLEM_BURGERS 2       /* problems.py:276-326 */
+#define FBP_PROBLEM_POISSON2D 3     /* new: -lap u = f, hard zero BC */
+#define FBP_PROBLEM_WAVE_C 4        /* problems.py:346-405, constant velocity */
+#define FBP_PROBLEM_HELMHOLTZ2D 5   /* new: -lap u - k^2 u = f, hard zero BC */
+
+typedef struct fbp_problem {
+    int32_t kind;
+    int32_t n_int;        /* integer parameter (Poisson: number of frequencies) */
+    float p[8];           /* scalar parameters, meaning per kind (see problems.py) */
+    const float* gauss;   /* (ng, 4) Gaussians [mx, my, sd, amp] (wave source, Helmholtz f) */
+    int32_t ng;
+} fbp_problem;
+
+/* ------------------------------------------------------------------ */
+/* Entry points                                                        */
+/* ------------------------------------------------------------------ */
+
+int fbp_abi_version(void);
+const char* fbp_last_error(void);
+
+/* Scratch for fbp_scan_i32 over n elements. */
+size_t fbp_scan_scratch_bytes(int64_t n);
+
+/* Exclusive prefix sum of int32 counts: out[0..n] with out[n] = total.
+ * Generic helper of the interaction-list build (the cumsum of
+ * fbpinns/decompositions_base.py:58). */
+int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n,
+                 void* scratch, size_t scratch_bytes, void* stream);
+
+/* Count pass of the point-in-box test.  For every point: the number of
+ * selected boxes that contain it (pt_count), the bit mask of their POU levels
+ * (pt_lvl) and its popcount (pt_nlvl).  model_count (nullable) receives the
+ * number of points inside each box.  Replaces _inside_sum_batch
+ * (fbpinns/decompositions_base.py:24-48) as used by inside_points /
+ * inside_models (fbpinns/decompositions.py:202-215). */
+int fbp_inside_count(const float* x, int64_t n, const fbp_boxes* boxes,
+                     int32_t* pt_count, int32_t* pt_nlvl, uint64_t* pt_lvl,
+                     int32_t* model_count, void* stream);
+
+/* Fill pass: writes the interaction lists in the reference's point-major,
+ * box-minor order (n_take, m_take = box id) and the unique (point, level)
+ * slots (p_take, np_take) in the order of
+ * jnp.unique(stack(n_take, pou[m_take]), axis=0, return_inverse=True).
+ * pt_off / np_off are the exclusive scans of pt_count / pt_nlvl (n+1 long).
+ * Replaces _inside_take_batch (fbpinns/decompositions_base.py:51-68) and the
+ * POU unique of get_inputs (fbpinns/trainers.py:379-388). */
+int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes,
+                    const int32_t* pt_off, const int32_t* np_off, const uint64_t* pt_lvl,
+                    int32_t* n_take, int32_t* m_take, int32_t* p_take, int32_t* np_take,
+                    int64_t s_cap, int64_t u_cap, int32_t* status, void* stream);
+
+/* out[i] = inv[in[i]] for i < *count_dev (or < n when count_dev is NULL):
+ * the re-index of m_take to positions in all_ims = [active; fixed]
+ * (fbpinns/trainers.py:367-372). */
+int fbp_gather_i32(const int32_t* in, int64_t n, const int32_t* count_dev,
+                   const int32_t* inv, int32_t* out, void* stream);
+
+/* Flag compaction: out receives, in ascending order, every i < n with
+ * flag[i] != 0 (i.e. jnp.arange(n)[flag]); *count_dev = how many.
+ * Used for inside_ips / training_ips (fbpinns/decompositions_base.py:81,
+ * fbpinns/trainers.py:487). */
+size_t fbp_compact_scratch_bytes(int64_t n);
+int fbp_compact_flags(const int32_t* flag, int64_t n, int32_t* out, int32_t* count_dev,
+                      void* scratch, size_t scratch_bytes, void* stream);
+
+/* Stable counting sort of the point-major pairs by subdomain: for each
+ * subdomain its pairs in ascending point order.  Writes sd_start (m+1),
+ * sd_pair, sd_point, sd_slot.  s_dev is the device pair count (pt_off[n]).
+ * No reference counterpart: the reference gathers per-pair parameter copies
+ * (fbpinns/trainers.py:141-145) instead of grouping pairs by subdomain. */
+size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m);
+int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
+                   const int32_t* s_dev, int64_t s_cap, int64_t m,
+                   int32_t* sd_start, int32_t* sd_pair, int32_t* sd_point, int32_t* sd_slot,
+                   void* scratch, size_t scratch_bytes, void* stream);
+
+/* Work queue: each subdomain with select[j] != 0 (NULL = all) contributes
+ * ceil(count/chunk) items (subdomain, begin, count) in subdomain order.
+ * Also writes item_start (m+1): the first item of each subdomain. */
+size_t fbp_work_scratch_bytes(int64_t m);
+int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t* select, int32_t chunk,
+                   int32_t* items, int32_t* item_start, int32_t* n_items, int64_t items_cap,
+                   int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
+
+/* Per-pair forward jets: for every pair in the work items, the jets of
+ * u_j(x) * w_j(x) and of w_j(x) (J + J floats at pair_out[pair*2J]), where
+ * u_j = unnorm(FCN_j(norm(x))) and w_j is the cosine window.
+ * Replaces the vmapped FBPINN_model_inner under nested jvp
+ * (fbpinns/trainers.py:113-118,158, 219-227; networks.py:61-68;
+ * decompositions.py:184-199; windows.py:25-35). */
+int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs,
+                      float* pair_out, int32_t grid, void* stream);
+
+/* POU combination per point (the two segment sums and the divide of
+ * fbpinns/trainers.py:162-170, on jets by the quotient rule):
+ *   slot_out[u] = (U_l jets, W_l jets) of each (point, level) slot,
+ *   U[p]        = sum over levels of U_l / npou  (n x J).               */
+int fbp_pou_forward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou,
+                    const int32_t* pt_off, const int32_t* p_take, const float* pair_out,
+                    float* slot_out, float* U, int32_t* status, void* stream);
+
+/* Adjoint of fbp_pou_forward: from dL/dU (n x J) to the per-slot seeds
+ * dL/dN_l (written into the first J floats of each slot record). */
+int fbp_pou_backward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou,
+                     const int32_t* np_off, const float* U_bar, float* slot_out, void* stream);
+
+/* Fused POU + constraining operator + residual + loss (built-in problems):
+ * forward POU, hard-constraint ansatz jets, PDE residual, FP64 per-block
+ * sums of residual^2 (loss_part), and the seeds dL/dN_l per slot (written
+ * into slot_out).  The loss is mean(residual^2) over the n points
+ * (problems.py loss_fn's).  U_out (nullable) receives the constrained jets.
+ * Replaces constraining_fn + loss_fn inside FBPINN_loss
+ * (fbpinns/trainers.py:174, 249-267). */
+int fbp_pou_loss(int32_t xd, int32_t d2mask, const fbp_problem* prob,
+                 int64_t n, int32_t npou, const float* x,
+                 const int32_t* pt_off, const int32_t* np_off, const int32_t* p_take,
+                 const float* pair_out, float* slot_out, float* U_out,
+                 double* loss_part, int32_t n_part, int32_t* status, void* stream);
+
+/* Deterministic sum of the n_part FP64 partials, times scale. */
+int fbp_loss_finalize(const double* loss_part, int32_t n_part, double scale,
+                      double* loss, void* stream);
+
+/* Per-pair adjoint: recomputes the forward jets per pair in registers and
+ * back-propagates the slot seeds through window product, unnormalisation and
+ * the FCN jet, writing one gradient partial (P floats) per work item.
+ * Replaces XLA's reverse-mode transpose of the model under value_and_grad
+ * (fbpinns/trainers.py:292). */
+int fbp_adjoint_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs,
+                      const float* slot_out, float* grad_part, int32_t grid, void* stream);
+
+/* grad[j] = sum of the partials of subdomain j's items, in item order. */
+int fbp_grad_reduce(const float* grad_part, const int32_t* item_start, int64_t m,
+                    int32_t nparam, float* grad, void* stream);
+
+/* Adam (optax.adam defaults and ordering, the shared step count) applied to
+ * rows j with state[j] == 1 only; other rows untouched.  count_dev is the
+ * int32 step count, incremented on the device.  Replaces optax.adam update +
+ * apply_updates (fbpinns/trainers.py:294-295, 430-431). */
+int fbp_adam(float* theta, float* m1, float* m2, const float* grad, const uint8_t* state,
+             int64_t m, int32_t nparam, float lr, float b1, float b2, float eps, float eps_root,
+             int32_t* count_dev, void* stream);
+
+/* Uniform points in the box [xmin, xmax] (host arrays, xd values) from a
+ * counter-based Philox-4x32-10 stream (seed, offset): x = xmin + (xmax-xmin)*u
+ * as in fbpinns/domains.py:136-140 (sampler "uniform"). */
+int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, const double* xmax,
+                       uint64_t seed, uint64_t offset, void* stream);
+
+/* FP32 FMA throughput probe used for the roofline denominator: runs
+ * `iters` dependent-chain FMA loops on every SM; *flops_out (host) gets the
+ * flop count of the launch. */
+int fbp_fma_probe(float* sink, int32_t blocks, int32_t iters, double* flops_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FBPGPU_H */
