@@ -42,7 +42,7 @@ class Net(C.Structure):
 
 class Pairs(C.Structure):
     _fields_ = [("sd_start", C.c_void_p), ("sd_pair", C.c_void_p), ("sd_point", C.c_void_p), ("sd_slot", C.c_void_p),
-                ("items", C.c_void_p), ("n_items", C.c_void_p), ("items_cap", C.c_int64)]
+                ("items", C.c_void_p), ("n_items", C.c_void_p), ("items_cap", C.c_int64), ("slots_cap", C.c_int64)]
 
 
 class Problem(C.Structure):
@@ -68,17 +68,17 @@ _SIG = {
     "fbp_work_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_build_work": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, C.c_size_t, _P]),
     "fbp_forward_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _I32, _P]),
-    "fbp_pou_forward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _P, _P, _P, _P]),
-    "fbp_pou_backward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _P]),
-    "fbp_pou_loss": (C.c_int, [_I32, _I32, C.POINTER(Problem), _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _I32,
-                               _P, _P]),
+    "fbp_pou_forward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _P]),
+    "fbp_pou_backward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _P]),
+    "fbp_pou_loss": (C.c_int, [_I32, _I32, C.POINTER(Problem), _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _I64, _I64,
+                               _P, _I32, _P, _P]),
     "fbp_loss_finalize": (C.c_int, [_P, _I32, C.c_double, _P, _P]),
     "fbp_adjoint_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _P, _I32, _P]),
     "fbp_grad_reduce": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "fbp_adam": (C.c_int, [_P, _P, _P, _P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                            _P, _P]),
     "fbp_sample_uniform": (C.c_int, [_P, _I64, _I32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64,
-                                     C.c_uint64, _P]),
+                                     C.c_uint64, _P, _P]),
     "fbp_fma_probe": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_double), _P]),
 }
 

@@ -379,8 +379,9 @@ __global__ void __launch_bounds__(AdjT<C>::T) adjoint_pairs_kernel(fbp_net net, 
                 float w[J];
                 window_jet<C>(S, xn, w);
                 float nb[J];
+                const bool ok = slot >= 0 && slot < pr.slots_cap;  // overflowed slots carry no seed
 #pragma unroll
-                for (int c = 0; c < J; ++c) nb[c] = slot_out[(size_t)slot * (2 * J) + c];
+                for (int c = 0; c < J; ++c) nb[c] = ok ? slot_out[(size_t)slot * (2 * J) + c] : 0.f;
                 // adjoint of uw = u (*) w with w constant: u-bar = M_w^T N-bar
                 float ub[J];
                 ub[0] = nb[0] * w[0];

@@ -32,10 +32,9 @@ int sm_count() {
 // ---------------------------------------------------------------------------
 // Adam, masked by the scheduler state (1 = active).  optax.adam: scale_by_adam
 // (mu, nu moments, count incremented, bias corrections) then scale(-lr), then
-// apply_updates.  The count is a shared device scalar, incremented once per
-// call by block 0 / thread 0 after every block has read it: each block reads
-// *count before the grid-wide increment would be visible only because the
-// increment is done by a separate tiny kernel that runs after this one.
+// apply_updates.  Every thread reads the shared device count and uses count+1
+// for the bias corrections; a separate one-thread kernel launched after this
+// one stores the increment, so no block can see a half-updated count.
 // ---------------------------------------------------------------------------
 __global__ void adam_kernel(float* __restrict__ theta, float* __restrict__ m1, float* __restrict__ m2,
                             const float* __restrict__ grad, const uint8_t* __restrict__ state,
@@ -92,7 +91,8 @@ struct Box3 {
 };
 
 __global__ void sample_uniform_kernel(float* __restrict__ x, int64_t n, int xd, Box3 box, uint64_t seed,
-                                      uint64_t offset) {
+                                      uint64_t offset0, const int32_t* __restrict__ counter) {
+    const uint64_t offset = offset0 + (counter ? (uint64_t)(uint32_t)*counter : 0ull);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint4 r = philox4x32_10(
@@ -151,7 +151,7 @@ extern "C" int fbp_adam(float* theta, float* m1, float* m2, const float* grad, c
 }
 
 extern "C" int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, const double* xmax,
-                                  uint64_t seed, uint64_t offset, void* stream) {
+                                  uint64_t seed, uint64_t offset, const int32_t* counter, void* stream) {
     FBP_REQUIRE(x && xmin && xmax, FBP_ERR_INVALID, "fbp_sample_uniform: null pointer");
     FBP_REQUIRE(xd >= 1 && xd <= 3, FBP_ERR_INVALID, "fbp_sample_uniform: xd=%d not in 1..3", xd);
     FBP_REQUIRE(n >= 0, FBP_ERR_INVALID, "fbp_sample_uniform: n < 0");
@@ -163,7 +163,7 @@ extern "C" int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double*
     }
     int blocks = (int)((n + 255) / 256);
     if (blocks > sm_count() * 16) blocks = sm_count() * 16;
-    sample_uniform_kernel<<<blocks, 256, 0, as_stream(stream)>>>(x, n, xd, b, seed, offset);
+    sample_uniform_kernel<<<blocks, 256, 0, as_stream(stream)>>>(x, n, xd, b, seed, offset, counter);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
 }

@@ -278,23 +278,27 @@ struct PointPOU {
     // forward POU for point p; writes slot records; returns U (unconstrained)
     __device__ static void run(int64_t p, int npou, const int32_t* __restrict__ pt_off,
                                const int32_t* __restrict__ p_take, const float* __restrict__ pair_out,
-                               float* __restrict__ slot_out, float (&U)[J], int32_t* status) {
+                               float* __restrict__ slot_out, float (&U)[J], int64_t s_cap, int64_t u_cap,
+                               int32_t* status) {
         float N[J], W[J], Ul[J];
 #pragma unroll
         for (int c = 0; c < J; ++c) U[c] = 0.f;
-        const int e0 = pt_off[p], e1 = pt_off[p + 1];
+        const int e0 = (int)min((int64_t)pt_off[p], s_cap), e1 = (int)min((int64_t)pt_off[p + 1], s_cap);
         int cur = -1;
         for (int e = e0; e <= e1; ++e) {
             const int r = e < e1 ? p_take[e] : -2;
             if (r != cur) {
                 if (cur >= 0) {
                     quotient<XD, D2>(N, W, Ul);
-                    float* so = slot_out + (size_t)cur * (2 * J);
 #pragma unroll
-                    for (int c = 0; c < J; ++c) {
-                        U[c] += Ul[c];
-                        so[c] = Ul[c];
-                        so[J + c] = W[c];
+                    for (int c = 0; c < J; ++c) U[c] += Ul[c];
+                    if (cur < u_cap) {
+                        float* so = slot_out + (size_t)cur * (2 * J);
+#pragma unroll
+                        for (int c = 0; c < J; ++c) {
+                            so[c] = Ul[c];
+                            so[J + c] = W[c];
+                        }
                     }
                 }
                 if (r >= 0 && r < cur) atomicOr(status, FBP_STATUS_LEVEL_ORDER);
@@ -318,12 +322,13 @@ struct PointPOU {
 
     // seeds: dL/dU (point) -> dL/dN per slot (overwrites the U_l half of each record)
     __device__ static void seed(int64_t p, int npou, const int32_t* __restrict__ np_off, const float (&Ub)[J],
-                                float* __restrict__ slot_out) {
+                                float* __restrict__ slot_out, int64_t u_cap) {
         const float inv = 1.0f / (float)npou;
         float ubl[J];
 #pragma unroll
         for (int c = 0; c < J; ++c) ubl[c] = Ub[c] * inv;
-        for (int u = np_off[p]; u < np_off[p + 1]; ++u) {
+        const int u1 = (int)min((int64_t)np_off[p + 1], u_cap);
+        for (int u = np_off[p]; u < u1; ++u) {
             float* so = slot_out + (size_t)u * (2 * J);
             float W[J], Nb[J];
 #pragma unroll
@@ -340,11 +345,11 @@ __global__ void __launch_bounds__(POU_T) pou_forward_kernel(int64_t n, int npou,
                                                              const int32_t* __restrict__ p_take,
                                                              const float* __restrict__ pair_out,
                                                              float* __restrict__ slot_out, float* __restrict__ U,
-                                                             int32_t* status) {
+                                                             int64_t s_cap, int64_t u_cap, int32_t* status) {
     constexpr int J = JL<XD, D2>::J;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         float u[J];
-        PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, status);
+        PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, s_cap, u_cap, status);
 #pragma unroll
         for (int c = 0; c < J; ++c) U[p * J + c] = u[c];
     }
@@ -353,13 +358,13 @@ __global__ void __launch_bounds__(POU_T) pou_forward_kernel(int64_t n, int npou,
 template <int XD, int D2>
 __global__ void __launch_bounds__(POU_T) pou_backward_kernel(int64_t n, int npou, const int32_t* __restrict__ np_off,
                                                               const float* __restrict__ Ubar,
-                                                              float* __restrict__ slot_out) {
+                                                              float* __restrict__ slot_out, int64_t u_cap) {
     constexpr int J = JL<XD, D2>::J;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         float ub[J];
 #pragma unroll
         for (int c = 0; c < J; ++c) ub[c] = Ubar[p * J + c];
-        PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out);
+        PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out, u_cap);
     }
 }
 
@@ -385,13 +390,14 @@ __global__ void __launch_bounds__(POU_T) pou_loss_kernel(fbp_problem P, int64_t 
                                                           const int32_t* __restrict__ p_take,
                                                           const float* __restrict__ pair_out,
                                                           float* __restrict__ slot_out, float* __restrict__ U_out,
+                                                          int64_t s_cap, int64_t u_cap,
                                                           double* __restrict__ loss_part, int32_t* status) {
     constexpr int J = JL<XD, D2>::J;
     __shared__ double sh[POU_T / 32];
     double acc = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         float u[J];
-        PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, status);
+        PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, s_cap, u_cap, status);
         float xp[XD];
 #pragma unroll
         for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
@@ -431,7 +437,7 @@ __global__ void __launch_bounds__(POU_T) pou_loss_kernel(fbp_problem P, int64_t 
             ub[1 + d] += 2.0f * B[1 + d] * ucb[1 + XD + s];
             ub[1 + XD + s] = B[0] * ucb[1 + XD + s];
         }
-        PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out);
+        PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out, u_cap);
     }
     const double tot = block_sum_double(acc, sh);
     if (threadIdx.x == 0) loss_part[blockIdx.x] = tot;
@@ -477,14 +483,14 @@ using namespace fbp;
 
 extern "C" int fbp_pou_forward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou, const int32_t* pt_off,
                                const int32_t* p_take, const float* pair_out, float* slot_out, float* U,
-                               int32_t* status, void* stream) {
+                               int64_t s_cap, int64_t u_cap, int32_t* status, void* stream) {
     FBP_REQUIRE(pt_off && U && status && npou > 0, FBP_ERR_INVALID, "fbp_pou_forward: bad args");
     if (n == 0) return FBP_OK;
     cudaStream_t st = as_stream(stream);
     const int g = grid_pts(n);
 #define X(a, b)                                                                                                   \
     if (xd == a && d2mask == b) {                                                                                 \
-        pou_forward_kernel<a, b><<<g, POU_T, 0, st>>>(n, npou, pt_off, p_take, pair_out, slot_out, U, status); \
+        pou_forward_kernel<a, b><<<g, POU_T, 0, st>>>(n, npou, pt_off, p_take, pair_out, slot_out, U, s_cap, u_cap, status); \
         FBP_LAUNCH_CHECK();                                                                                       \
         return FBP_OK;                                                                                            \
     }
@@ -495,14 +501,14 @@ extern "C" int fbp_pou_forward(int32_t xd, int32_t d2mask, int64_t n, int32_t np
 }
 
 extern "C" int fbp_pou_backward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou, const int32_t* np_off,
-                                const float* U_bar, float* slot_out, void* stream) {
+                                const float* U_bar, float* slot_out, int64_t u_cap, void* stream) {
     FBP_REQUIRE(np_off && U_bar && npou > 0, FBP_ERR_INVALID, "fbp_pou_backward: bad args");
     if (n == 0) return FBP_OK;
     cudaStream_t st = as_stream(stream);
     const int g = grid_pts(n);
 #define X(a, b)                                                                                       \
     if (xd == a && d2mask == b) {                                                                     \
-        pou_backward_kernel<a, b><<<g, POU_T, 0, st>>>(n, npou, np_off, U_bar, slot_out);           \
+        pou_backward_kernel<a, b><<<g, POU_T, 0, st>>>(n, npou, np_off, U_bar, slot_out, u_cap);    \
         FBP_LAUNCH_CHECK();                                                                           \
         return FBP_OK;                                                                                \
     }
@@ -514,8 +520,8 @@ extern "C" int fbp_pou_backward(int32_t xd, int32_t d2mask, int64_t n, int32_t n
 
 extern "C" int fbp_pou_loss(int32_t xd, int32_t d2mask, const fbp_problem* prob, int64_t n, int32_t npou,
                             const float* x, const int32_t* pt_off, const int32_t* np_off, const int32_t* p_take,
-                            const float* pair_out, float* slot_out, float* U_out, double* loss_part, int32_t n_part,
-                            int32_t* status, void* stream) {
+                            const float* pair_out, float* slot_out, float* U_out, int64_t s_cap, int64_t u_cap,
+                            double* loss_part, int32_t n_part, int32_t* status, void* stream) {
     FBP_REQUIRE(prob && x && pt_off && np_off && loss_part && status && npou > 0, FBP_ERR_INVALID,
                 "fbp_pou_loss: bad args");
     FBP_REQUIRE(n > 0, FBP_ERR_INVALID, "fbp_pou_loss: no points");
@@ -527,7 +533,7 @@ extern "C" int fbp_pou_loss(int32_t xd, int32_t d2mask, const fbp_problem* prob,
 #define X(a, b)                                                                                              \
     if (xd == a && d2mask == b) {                                                                            \
         pou_loss_kernel<a, b><<<g, POU_T, 0, st>>>(*prob, n, npou, inv_n, x, pt_off, np_off, p_take, pair_out, \
-                                                    slot_out, U_out, loss_part, status);                    \
+                                                    slot_out, U_out, s_cap, u_cap, loss_part, status);      \
         FBP_LAUNCH_CHECK();                                                                                  \
         if (n_part > g) FBP_CUDA_CHECK(cudaMemsetAsync(loss_part + g, 0, (n_part - g) * sizeof(double), st)); \
         return FBP_OK;                                                                                       \

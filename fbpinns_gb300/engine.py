@@ -172,6 +172,7 @@ class PointSet:
         else:
             p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
         p.items_cap = self.items_cap
+        p.slots_cap = self.slot_out.shape[0]
         return p
 
     def check_status(self):
@@ -274,14 +275,16 @@ class FBPINNEngine:
         t = ps.takes
         _lib.check(lib.fbp_pou_forward(self.xd, self.d2mask, ps.n, self.npou, _lib.ptr(t.pt_off), _lib.ptr(t.p_take),
                                        _lib.ptr(ps.pair_out), _lib.ptr(ps.slot_out), _lib.ptr(ps.U),
-                                       _lib.ptr(t.status), _lib.stream_ptr(stream)), "fbp_pou_forward")
+                                       ps.pair_out.shape[0], ps.slot_out.shape[0], _lib.ptr(t.status),
+                                       _lib.stream_ptr(stream)), "fbp_pou_forward")
         return ps.U
 
     def pou_backward(self, ps, Ubar, stream=None):
         lib = _lib.load()
         Ubar = Ubar.to(torch.float32).contiguous()
         _lib.check(lib.fbp_pou_backward(self.xd, self.d2mask, ps.n, self.npou, _lib.ptr(ps.takes.np_off),
-                                        _lib.ptr(Ubar), _lib.ptr(ps.slot_out), _lib.stream_ptr(stream)),
+                                        _lib.ptr(Ubar), _lib.ptr(ps.slot_out), ps.slot_out.shape[0],
+                                        _lib.stream_ptr(stream)),
                    "fbp_pou_backward")
 
     def pou_loss(self, ps, U_out=None, stream=None):
@@ -292,7 +295,8 @@ class FBPINNEngine:
         st = _lib.stream_ptr(stream)
         _lib.check(lib.fbp_pou_loss(self.xd, self.d2mask, C.byref(self._problem), ps.n, self.npou, _lib.ptr(ps.x),
                                     _lib.ptr(t.pt_off), _lib.ptr(t.np_off), _lib.ptr(t.p_take), _lib.ptr(ps.pair_out),
-                                    _lib.ptr(ps.slot_out), _lib.ptr(U_out), _lib.ptr(self.loss_part),
+                                    _lib.ptr(ps.slot_out), _lib.ptr(U_out), ps.pair_out.shape[0], ps.slot_out.shape[0],
+                                    _lib.ptr(self.loss_part),
                                     self.loss_part.numel(), _lib.ptr(t.status), st), "fbp_pou_loss")
         _lib.check(lib.fbp_loss_finalize(_lib.ptr(self.loss_part), self.loss_part.numel(), 1.0 / ps.n,
                                          _lib.ptr(self.loss), st), "fbp_loss_finalize")
@@ -325,12 +329,13 @@ class FBPINNEngine:
         self.adam(lr, stream=stream, **adam_kw)
         return loss
 
-    def sample(self, x_out, seed, offset, xmin, xmax, stream=None):
+    def sample(self, x_out, seed, offset, xmin, xmax, counter=None, stream=None):
+        """Uniform points into x_out; the stream offset is offset + *counter."""
         lib = _lib.load()
         lo = (C.c_double * 3)(*[float(v) for v in xmin])
         hi = (C.c_double * 3)(*[float(v) for v in xmax])
-        _lib.check(lib.fbp_sample_uniform(_lib.ptr(x_out), x_out.shape[0], self.xd, lo, hi, seed, offset,
-                                          _lib.stream_ptr(stream)), "fbp_sample_uniform")
+        _lib.check(lib.fbp_sample_uniform(_lib.ptr(x_out), x_out.shape[0], self.xd, lo, hi, int(seed), int(offset),
+                                          _lib.ptr(counter), _lib.stream_ptr(stream)), "fbp_sample_uniform")
 
 
 class FBPINNJet(torch.autograd.Function):

@@ -1,0 +1,370 @@
+"""FBPINN trainer (the reference's ``fbpinns/trainers.py`` API) on the GPU engine.
+
+``FBPINNTrainer(c).train()`` follows the reference's loop
+(fbpinns/trainers.py:577-687): initialise parameters, iterate the scheduler,
+rebuild the training inputs when the active mask changes, take a step, and
+report (summary line, test L1, model pickles).  The step itself is one of:
+
+* ``FusedStep`` — built-in problems: the fused CUDA forward / POU / residual /
+  FP64 loss / adjoint / Adam sequence, optionally resampling the collocation
+  points on the device each step, captured in a CUDA graph;
+* ``GenericStep`` — any problem: ``FBPINNJet`` gives the per-point jets,
+  ``constraining_fn`` and ``loss_fn`` run in torch autograd on them, the
+  gradient comes back through the CUDA adjoint.
+"""
+
+import logging
+import os
+import pickle
+import sys
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import FBPINNEngine, FBPINNJet, constrained_jets, d2mask_of, jet_index
+from .networks import fcn_param_count, pack_layers, unpack_layers, FCN
+from .optim import adam_update
+from .takes import get_inputs, split_takes, inside_models, grid_of  # noqa: F401  (re-exported API)
+
+logger = logging.getLogger("fbpinns_gb300")
+if not logger.handlers:
+    _h = logging.StreamHandler(stream=sys.stdout)
+    _h.setFormatter(logging.Formatter(fmt="[%(levelname)s] %(asctime)s - %(message)s", datefmt="%Y-%m-%d %H:%M:%S"))
+    logger.addHandler(_h)
+    logger.setLevel(logging.INFO)
+
+
+def _to_dev(v, dev):
+    return v.to(dev) if torch.is_tensor(v) else v
+
+
+class GenericStep:
+    """Loss and gradients of any problem through the CUDA jets.
+
+    ``constraints`` are the per-constraint lists without ``required_ujs``
+    ([x_batch, *values]); their points are concatenated into one point set and
+    each constraint owns a contiguous row range (fbpinns/trainers.py:249-267).
+    """
+
+    def __init__(self, engine, problem, all_params, constraints, required_ujss, ps=None):
+        self.eng, self.problem, self.all_params = engine, problem, all_params
+        dev = engine.device
+        self.constraints = [[_to_dev(torch.as_tensor(c_), dev) if not torch.is_tensor(c_) else c_.to(dev)
+                             for c_ in con] for con in constraints]
+        self.required = required_ujss
+        self.sizes = [con[0].shape[0] for con in self.constraints]
+        self.offsets = np.cumsum([0] + self.sizes[:-1]).tolist()
+        x = torch.cat([con[0].float() for con in self.constraints]) if self.constraints else None
+        self.ps = ps if ps is not None else engine.points(x)
+        self.xd = engine.xd
+
+    def _trainable_problem(self):
+        tp = self.all_params.get("trainable", {}).get("problem", {})
+        return {k: v for k, v in tp.items() if torch.is_tensor(v)}
+
+    def loss(self, theta):
+        eng = self.eng
+        U = FBPINNJet.apply(theta, eng, self.ps)
+        cons_ = []
+        for ic, con in enumerate(self.constraints):
+            a, b = self.offsets[ic], self.offsets[ic] + self.sizes[ic]
+            x = self.ps.x[a:b]
+            Uc = constrained_jets(self.problem.constraining_fn, self.all_params, x, U[a:b], self.xd, eng.d2mask)
+            ujs = [Uc[:, k:k + 1] for k in (jet_index(self.xd, eng.d2mask, ixs) for _, ixs in self.required[ic])]
+            cons_.append(list(con) + ujs)
+        return self.problem.loss_fn(self.all_params, cons_)
+
+    def loss_and_grads(self, theta):
+        tp = self._trainable_problem()
+        leaves = [theta] + list(tp.values())
+        for v in tp.values():
+            v.requires_grad_(True)
+        loss = self.loss(theta)
+        gs = torch.autograd.grad(loss, leaves, allow_unused=True)
+        gs = [torch.zeros_like(l) if g is None else g for g, l in zip(gs, leaves)]
+        return loss.detach(), gs[0], dict(zip(tp.keys(), gs[1:]))
+
+    def step(self, opt):
+        eng = self.eng
+        theta = eng.theta.detach().clone().requires_grad_(True)
+        loss, gtheta, gprob = self.loss_and_grads(theta)
+        count = int(eng.count.item())
+        tp = self._trainable_problem()
+        if tp:
+            if not hasattr(self, "_pm"):
+                self._pm = {k: (torch.zeros_like(v), torch.zeros_like(v)) for k, v in tp.items()}
+            with torch.no_grad():
+                for k, v in tp.items():
+                    m1, m2 = self._pm[k]
+                    adam_update(v, gprob[k], m1, m2, count, opt["learning_rate"], opt["b1"], opt["b2"], opt["eps"],
+                                opt["eps_root"])
+        eng.adam(opt["learning_rate"], opt["b1"], opt["b2"], opt["eps"], opt["eps_root"], grad=gtheta)
+        return loss
+
+
+class FusedStep:
+    """The fused CUDA step for a built-in problem.
+
+    ``x`` fixes the collocation points; alternatively ``resample=(n, xmin,
+    xmax, seed)`` draws n new uniform points on the device every step (offset
+    by the device step count) and rebuilds the interaction lists into
+    fixed-capacity buffers, so the whole step has no host synchronisation and
+    is captured in a CUDA graph when ``use_graph``.
+    """
+
+    def __init__(self, engine, spec, opt, x=None, resample=None, use_graph=True, headroom=1.25):
+        self.eng, self.opt = engine, opt
+        engine.set_problem(spec)
+        self.resample = resample
+        self.use_graph = use_graph
+        self.graph = None
+        self.h2d_src = None
+        if resample is not None:
+            n, xmin, xmax, seed = resample
+            self.xmin, self.xmax, self.seed = list(xmin), list(xmax), int(seed)
+            x0 = torch.empty((n, engine.xd), dtype=torch.float32, device=engine.device)
+            engine.sample(x0, self.seed, 1 << 32, self.xmin, self.xmax)
+            probe = engine.points(x0)
+            s, u = probe.s, probe.u
+            caps = (int(s * headroom) + 1024, int(u * headroom) + 1024)
+            del probe
+            self.ps = engine.points(x0, caps=caps)
+        else:
+            self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(engine.device))
+
+    def set_state(self, active):
+        self.eng.set_state(active)
+        self.ps.build_work()
+
+    def _body(self, stream=None):
+        eng, o = self.eng, self.opt
+        if self.resample is not None:
+            eng.sample(self.ps.x, self.seed, 0, self.xmin, self.xmax, counter=eng.count, stream=stream)
+            self.ps.rebuild(stream=stream)
+        elif self.h2d_src is not None:
+            self.ps.x.copy_(self.h2d_src, non_blocking=True)
+            self.ps.rebuild(stream=stream)
+        return eng.fused_step(self.ps, o["learning_rate"], stream=stream, b1=o["b1"], b2=o["b2"], eps=o["eps"],
+                              eps_root=o["eps_root"])
+
+    def capture(self, warmup=2):
+        """Capture one step in a CUDA graph (after ``warmup`` eager steps on a side stream)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(warmup):
+                self._body()
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._body()
+        self.graph = g
+
+    def step(self):
+        if self.use_graph:
+            if self.graph is None:
+                self.capture()
+            self.graph.replay()
+        else:
+            self._body()
+        return self.eng.loss
+
+    def check(self):
+        self.ps.check_status()
+
+
+def init_subdomain_networks(network, kwargs, m, seed):
+    """Per-subdomain network init from split seeds (fbpinns/trainers.py:601-607)."""
+    g = torch.Generator().manual_seed(int(seed))
+    seeds = torch.randint(0, 2 ** 62, (m,), generator=g).tolist()
+    per = [network.init_params(s, **kwargs) for s in seeds]
+    static = per[0][0]
+    layers = [tuple(torch.stack([p[1]["layers"][li][k] for p in per]) for k in range(len(per[0][1]["layers"][li])))
+              for li in range(len(per[0][1]["layers"]))]
+    return static, {"layers": layers}
+
+
+class FBPINNTrainer:
+    """``FBPINNTrainer(c).train() -> all_params`` (fbpinns/trainers.py:479-774)."""
+
+    def __init__(self, c):
+        self.c = c
+        if getattr(c, "save_models", False):
+            c.get_outdirs()
+            c.save_constants_file()
+        self.u_test_losses = []
+        self.history = []
+
+    def _print_summary(self, i, loss, rate, start):
+        logger.info("[i: %i/%i] loss: %.4f rate: %.1f elapsed: %.2f hr %s" % (
+            i, self.c.n_steps, loss, rate, (time.time() - start) / 3600, self.c.run))
+        self.history.append({"i": i, "loss": loss, "rate": rate})
+
+    def _save_model(self, i, model):
+        with open(self.c.model_out_dir + f"model_{i:08d}.jax", "wb") as f:
+            pickle.dump(model, f)
+
+    def train(self):
+        c = self.c
+        dev = torch.device(c.device)
+        torch.manual_seed(c.seed)
+        np.random.seed(c.seed)
+        all_params = {"static": {}, "trainable": {}}
+        domain, problem, decomposition = c.domain, c.problem, c.decomposition
+        for tag, cl, kw in zip(["domain", "problem", "decomposition"], [domain, problem, decomposition],
+                               [c.domain_init_kwargs, c.problem_init_kwargs, c.decomposition_init_kwargs]):
+            ps_ = cl.init_params(**kw)
+            if ps_[0]:
+                all_params["static"][tag] = ps_[0]
+            if ps_[1]:
+                all_params["trainable"][tag] = ps_[1]
+        st_dec = all_params["static"]["decomposition"]
+        m, xd = st_dec["m"], st_dec["xd"]
+        assert all_params["static"]["domain"]["xd"] == all_params["static"]["problem"]["dims"][1] == xd
+        logger.info(f"Total number of subdomains: {m}")
+        if c.network is not FCN:
+            raise NotImplementedError("the compiled jet kernels implement the FCN network")
+        net_static, net_tr = init_subdomain_networks(c.network, c.network_init_kwargs, m, c.seed)
+        layer_sizes = list(c.network_init_kwargs["layer_sizes"])
+        scheduler = c.scheduler(all_params=all_params, n_steps=c.n_steps, **c.scheduler_kwargs)
+
+        # constraints (sampled once, as the reference does; or resampled per step)
+        constraints_global = problem.sample_constraints(all_params=all_params, domain=domain, key=c.seed,
+                                                        sampler=c.sampler, batch_shapes=c.ns)
+        required = [con[-1] for con in constraints_global]
+        constraints_global = [con[:-1] for con in constraints_global]
+        d2 = d2mask_of(required, xd)
+        eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid)
+        eng.set_theta(pack_layers(net_tr["layers"]))
+        for k, v in list(all_params["trainable"].get("problem", {}).items()):
+            all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()
+        all_params["static"]["problem"] = {k: _to_dev(v, dev) for k, v in all_params["static"]["problem"].items()}
+        opt = c.optimiser(**c.optimiser_kwargs)
+        spec = problem.fused_spec(all_params) if c.engine == "fused" else None
+        use_fused = (spec is not None and len(constraints_global) == 1
+                     and not all_params["trainable"].get("problem"))
+        if c.resample and not use_fused:
+            raise NotImplementedError("resampling per step is implemented for the fused built-in problems")
+
+        # test data (fbpinns/trainers.py:463-470, 620-624)
+        x_test = domain.sample_interior(all_params, None, "grid", c.n_test)
+        u_exact = problem.exact_solution(all_params, x_test, c.n_test)
+        self.x_test, self.u_exact = x_test, u_exact
+        self.engine, self.all_params = eng, all_params
+        ps_test = None
+
+        x_global = torch.cat([con[0] for con in constraints_global]).float()
+        sizes = [con[0].shape[0] for con in constraints_global]
+        offs = np.cumsum([0] + sizes)
+        step = None
+        start0 = start1 = time.time()
+        report_time = 0.0
+        lossval = None
+        for i, active_ in enumerate(scheduler):
+            if active_ is not None:
+                t0 = time.time()
+                active = np.array(active_).copy()
+                # points inside models with raw state 1 (fbpinns/trainers.py:482-507)
+                ims = np.arange(m)[active == 1]
+                if use_fused and c.resample:
+                    training_x, cons = None, None
+                else:
+                    ips = inside_models(st_dec, x_global, ims)[0].long().cpu()
+                    training_x = x_global[ips]
+                    cons = []
+                    for ic, con in enumerate(constraints_global):
+                        sel = ips[(ips >= offs[ic]) & (ips < offs[ic + 1])] - offs[ic]
+                        cons.append([v[sel] if torch.is_tensor(v) and v.shape[:1] == con[0].shape[:1] else v
+                                     for v in con])
+                # active/fixed masks after the training-point cut (fbpinns/trainers.py:347-357)
+                xs_for_mask = training_x if training_x is not None else None
+                state = active.copy()
+                state[state == 0] = 1
+                if xs_for_mask is not None and xs_for_mask.shape[0]:
+                    tk = eng.points(xs_for_mask.to(dev))
+                    has = (tk.takes.model_count > 0).cpu().numpy()
+                    del tk
+                else:
+                    has = np.ones(m, dtype=bool)
+                state = state * has
+                eng.set_state(state)
+                if use_fused:
+                    if step is None:
+                        res = None
+                        if c.resample:
+                            d = all_params["static"]["domain"]
+                            res = (int(np.prod(c.ns[0])), d["xmin"].tolist(), d["xmax"].tolist(), c.seed)
+                        step = FusedStep(eng, spec, opt, x=training_x, resample=res, use_graph=c.use_graph,
+                                         headroom=c.pair_headroom)
+                    else:
+                        if training_x is not None:
+                            step = FusedStep(eng, spec, opt, x=training_x, use_graph=c.use_graph)
+                        else:
+                            step.set_state(state)
+                else:
+                    step = GenericStep(eng, problem, all_params, cons, required)
+                logger.info(f"[i: {i}/{c.n_steps}] Updating active inputs done ({time.time() - t0:.2f} s)")
+            if i == 0:
+                self._test(i, eng, all_params, problem)
+            lossval = step.step(opt) if isinstance(step, GenericStep) else step.step()
+            i1 = i + 1
+            if i1 % c.summary_freq == 0:
+                lv = float(lossval.item())
+                rate = c.summary_freq / max(time.time() - start1 - report_time, 1e-9)
+                self._print_summary(i1, lv, rate, start0)
+                start1, report_time = time.time(), 0.0
+            if i1 % c.test_freq == 0 or (c.save_models and i1 % c.model_save_freq == 0):
+                t2 = time.time()
+                if i1 % c.test_freq == 0:
+                    self._test(i1, eng, all_params, problem)
+                if c.save_models and i1 % c.model_save_freq == 0:
+                    self._save_model(i1, self.model_tuple(i1, eng, all_params))
+                report_time += time.time() - t2
+        if isinstance(step, FusedStep):
+            torch.cuda.synchronize()
+            step.check()
+        all_params["trainable"]["network"] = {"subdomain": {"layers": [
+            (w.detach().cpu().clone(), b.detach().cpu().clone()) for w, b in unpack_layers(eng.theta, layer_sizes)]}}
+        if net_static:
+            all_params["static"]["network"] = {"subdomain": net_static}
+        logger.info(f"[i: {c.n_steps}/{c.n_steps}] Training complete")
+        return all_params
+
+    def model_tuple(self, i, eng, all_params):
+        """(i, all_params, all_opt_states, active, u_test_losses) as numpy, the
+        layout of the reference's model pickles (fbpinns/trainers.py:721)."""
+        ls = list(self.c.network_init_kwargs["layer_sizes"])
+        layers = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.theta, ls)]
+        mu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m1, ls)]
+        nu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m2, ls)]
+        ap = {"static": all_params["static"], "trainable": {"network": {"subdomain": {"layers": layers}}}}
+        opt = {"count": int(eng.count.item()), "mu": {"network": {"subdomain": {"layers": mu}}},
+               "nu": {"network": {"subdomain": {"layers": nu}}}}
+        return (i, ap, opt, eng.state.cpu().numpy().astype(int), np.array(self.u_test_losses))
+
+    def _test(self, i, eng, all_params, problem):
+        """Test L1 on the grid test points (fbpinns/trainers.py:727-765)."""
+        u_test = self.predict(eng, all_params, problem, self.x_test)
+        ue = torch.as_tensor(self.u_exact).reshape(-1, 1).to(u_test.device).float()
+        l1 = torch.mean(torch.abs(ue - u_test)).item()
+        l1n = l1 / ue.std().item()
+        self.u_test_losses.append([i, l1, l1n])
+        logger.info(f"[i: {i}/{self.c.n_steps}] test L1: {l1:.4e} (normalised {l1n:.4e})")
+        return l1
+
+    @staticmethod
+    def predict(eng, all_params, problem, x):
+        """FBPINN solution at points x with all subdomains (the test-step inference)."""
+        x = torch.as_tensor(x, dtype=torch.float32).to(eng.device)
+        key = "_test_points"
+        cache = getattr(eng, key, None)
+        if cache is None or cache[0] is not x and not torch.equal(cache[0], x):
+            ps = eng.points(x)
+            setattr(eng, key, (x, ps))
+        ps = getattr(eng, key)[1]
+        with torch.no_grad():
+            eng.forward_pairs(ps)
+            U = eng.pou_forward(ps)
+            return problem.constraining_fn(all_params, x, U[:, 0:1])

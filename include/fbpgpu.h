@@ -108,6 +108,7 @@ typedef struct fbp_pairs {
     const int32_t* items;     /* (cap, 3) work items: (subdomain, begin, count) */
     const int32_t* n_items;   /* device count of valid items */
     int64_t items_cap;
+    int64_t slots_cap;        /* rows of the slot buffer; larger slot ids are skipped */
 } fbp_pairs;
 
 /* Built-in PDE residuals fused into the POU/loss kernel. */
@@ -212,24 +213,29 @@ int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs
  *   U[p]        = sum over levels of U_l / npou  (n x J).               */
 int fbp_pou_forward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou,
                     const int32_t* pt_off, const int32_t* p_take, const float* pair_out,
-                    float* slot_out, float* U, int32_t* status, void* stream);
+                    float* slot_out, float* U, int64_t s_cap, int64_t u_cap,
+                    int32_t* status, void* stream);
 
 /* Adjoint of fbp_pou_forward: from dL/dU (n x J) to the per-slot seeds
  * dL/dN_l (written into the first J floats of each slot record). */
 int fbp_pou_backward(int32_t xd, int32_t d2mask, int64_t n, int32_t npou,
-                     const int32_t* np_off, const float* U_bar, float* slot_out, void* stream);
+                     const int32_t* np_off, const float* U_bar, float* slot_out, int64_t u_cap,
+                     void* stream);
 
 /* Fused POU + constraining operator + residual + loss (built-in problems):
  * forward POU, hard-constraint ansatz jets, PDE residual, FP64 per-block
  * sums of residual^2 (loss_part), and the seeds dL/dN_l per slot (written
  * into slot_out).  The loss is mean(residual^2) over the n points
  * (problems.py loss_fn's).  U_out (nullable) receives the constrained jets.
+ * Pairs at or beyond s_cap and slots at or beyond u_cap (capacity overflow,
+ * already flagged by fbp_inside_fill) are skipped.
  * Replaces constraining_fn + loss_fn inside FBPINN_loss
  * (fbpinns/trainers.py:174, 249-267). */
 int fbp_pou_loss(int32_t xd, int32_t d2mask, const fbp_problem* prob,
                  int64_t n, int32_t npou, const float* x,
                  const int32_t* pt_off, const int32_t* np_off, const int32_t* p_take,
                  const float* pair_out, float* slot_out, float* U_out,
+                 int64_t s_cap, int64_t u_cap,
                  double* loss_part, int32_t n_part, int32_t* status, void* stream);
 
 /* Deterministic sum of the n_part FP64 partials, times scale. */
@@ -257,10 +263,12 @@ int fbp_adam(float* theta, float* m1, float* m2, const float* grad, const uint8_
              int32_t* count_dev, void* stream);
 
 /* Uniform points in the box [xmin, xmax] (host arrays, xd values) from a
- * counter-based Philox-4x32-10 stream (seed, offset): x = xmin + (xmax-xmin)*u
- * as in fbpinns/domains.py:136-140 (sampler "uniform"). */
+ * counter-based Philox-4x32-10 stream (seed, offset + *counter): x = xmin +
+ * (xmax-xmin)*u as in fbpinns/domains.py:136-140 (sampler "uniform").
+ * counter (nullable, device int32) lets a captured graph draw new points on
+ * every replay (e.g. the Adam step count). */
 int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, const double* xmax,
-                       uint64_t seed, uint64_t offset, void* stream);
+                       uint64_t seed, uint64_t offset, const int32_t* counter, void* stream);
 
 /* FP32 FMA throughput probe used for the roofline denominator: runs
  * `iters` dependent-chain FMA loops on every SM; *flops_out (host) gets the

@@ -1,0 +1,80 @@
+"""Shared builders for the parity tests: the same decomposition, weights and
+points for the CUDA engine (float32) and the CPU oracle (float64)."""
+
+import numpy as np
+import torch
+
+from conftest import golden
+from fbpinns_gb300.constants import get_subdomain_ws
+from fbpinns_gb300 import decompositions as D
+from fbpinns_gb300.networks import pack_layers
+from oracle import model as OM
+
+
+def decomposition(recipe):
+    """Product static decomposition params for a named recipe (float32 tensors)."""
+    if recipe in ("ho", "ho2c", "ho_hardbc"):
+        sx = [np.linspace(0, 1, 15)]
+        return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.0), (0., 1.))[0]
+    if recipe.startswith("burgers"):
+        sx = [np.linspace(-1, 1, 16), np.linspace(0, 1, 8)]
+        return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.9), (0., 1.))[0]
+    if recipe in ("multilevel", "multilevel4"):
+        sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8)]
+        sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
+        return D.MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
+    if recipe == "poisson":
+        sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8, 16, 32)]
+        sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
+        return D.MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
+    if recipe in ("wave", "wave3d"):
+        sx = [np.linspace(-1, 1, 5), np.linspace(-1, 1, 4), np.linspace(0, 1, 3)]
+        return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.0), (0.5, 2.0))[0]
+    raise KeyError(recipe)
+
+
+def boxes_static(xmin, xmax, pou=None):
+    """A static decomposition dict from raw boxes (flag 1, unnorm (0,1))."""
+    m, xd = xmin.shape
+    z = torch.zeros((m, xd))
+    pou = torch.zeros((m, 1)) if pou is None else torch.as_tensor(pou, dtype=torch.float32).reshape(m, 1)
+    params = [torch.as_tensor(xmin), torch.as_tensor(xmax), z, z, torch.ones((m, 1)),
+              torch.tensor([[0.0, 1.0]]).repeat(m, 1)]
+    return {"m": m, "xd": xd, "subdomain": {"params": params, "pou": pou}}
+
+
+def golden_layers(g):
+    out, i = [], 0
+    while f"W{i}" in g:
+        out.append((torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])))
+        i += 1
+    return out
+
+
+def layer_sizes(layers):
+    return [layers[0][0].shape[2]] + [w.shape[1] for w, _ in layers]
+
+
+def oracle_params(static, layers64, problem=None):
+    """Oracle parameter dict (float64) from the product static params."""
+    p = static["subdomain"]["params"]
+    P = {"xmins": p[0].double(), "xmaxs": p[1].double(), "flags": p[4].double(), "unnorms": p[5].double(),
+         "pou": static["subdomain"]["pou"].double(), "layers": [(w.double(), b.double()) for w, b in layers64],
+         "problem": problem or {}, "problem_trainable": {}}
+    return P
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def random_layers(sizes, m, seed):
+    g = torch.Generator().manual_seed(seed)
+    out = []
+    for fi, fo in zip(sizes[:-1], sizes[1:]):
+        v = 1.0 / np.sqrt(fi)
+        out.append(((torch.rand((m, fo, fi), generator=g, dtype=torch.float64) * 2 - 1) * v,
+                    (torch.rand((m, fo), generator=g, dtype=torch.float64) * 2 - 1) * v))
+    return out

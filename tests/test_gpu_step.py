@@ -1,0 +1,223 @@
+"""Per-point jets, fused loss, adjoint gradient and Adam on the GPU against the
+reference's golden vectors and the float64 oracle.
+
+Tolerances (FP32 kernels vs FP64 oracle), stated per check: jets and loss
+1e-5 relative to the component's max magnitude; gradients 1e-4 relative to
+each subdomain-parameter block's max magnitude (sums over ~1e3-1e4 pairs in
+FP32)."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from helpers import decomposition, golden_layers, layer_sizes, oracle_params, rel_err, random_layers
+from oracle import model as OM
+from oracle import problems as OP
+from oracle import takes as OT
+from fbpinns_gb300.engine import FBPINNEngine, FBPINNJet, constrained_jets, jet_index, d2mask_of
+from fbpinns_gb300.networks import pack_layers
+from fbpinns_gb300 import problems as PR
+
+pytestmark = pytest.mark.gpu
+
+JET_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+def _engine(static, layers, d2mask, chunk=64):
+    eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk)
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    return eng
+
+
+@pytest.mark.parametrize("tag,dims,d2", [("ho_hardbc", [0], 1), ("burgers", [0, 1], 1), ("wave", [0, 1, 2], 7),
+                                         ("multilevel", [0, 1], 3)])
+def test_jets_vs_reference_golden(cuda, tag, dims, d2):
+    """POU-combined network jets (before the constraint) vs the reference's
+    forward values and their float64 finite differences."""
+    g = golden(f"model_{tag}.npz")
+    static = decomposition(tag)
+    layers = golden_layers(g)
+    eng = _engine(static, layers, d2)
+    ps = eng.points(torch.tensor(g["x_batch"], dtype=torch.float32))
+    U = FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy()
+    xd = len(static["subdomain"]["params"][0][0])
+    assert rel_err(U[:, 0:1], g["u_raw"]) < JET_TOL
+    for d in range(xd):
+        assert rel_err(U[:, 1 + d:2 + d], g[f"raw_d{d}"]) < JET_TOL, d
+        if (d2 >> d) & 1:
+            k = jet_index(xd, d2, (d, d))
+            assert rel_err(U[:, k:k + 1], g[f"raw_d{d}{d}"]) < JET_TOL, (d, d)
+
+
+CASES = {
+    # name: (recipe, layer sizes, problem class (product), product init kwargs, oracle class, oracle params, d2)
+    "ho_hardbc": ("ho_hardbc", [1, 32, 32, 1], PR.HarmonicOscillator1DHardBC, dict(d=2, w0=80, sd=0.1),
+                  OP.HarmonicOscillator1DHardBC, {"sd": 0.1, "mu": 4, "k": 6400}, 1),
+    "burgers": ("burgers", [2, 16, 16, 1], PR.BurgersEquation2D, dict(),
+                OP.BurgersEquation2D, {"sd": 0.1, "nu": 0.01 / math.pi}, 1),
+    "poisson": ("multilevel", [2, 8, 8, 1], PR.Poisson2D, dict(n_freq=6, sd=0.1),
+                OP.Poisson2D, {"sd": 0.1, "n_freq": 6}, 3),
+    "wave": ("wave", [3, 8, 8, 1], PR.WaveEquationConstantVelocity3D,
+             dict(c0=1.0, source=np.array([[0.1, -0.2, 0.3, 1.0], [-0.3, 0.2, 0.25, 0.5]])),
+             OP.WaveEquationConstantVelocity3D,
+             {"c0": 1.0, "source": torch.tensor([[0.1, -0.2, 0.3, 1.0], [-0.3, 0.2, 0.25, 0.5]], dtype=torch.float64)}, 7),
+    "helmholtz": ("multilevel", [2, 32, 32, 1], PR.Helmholtz2D, dict(k=8 * math.pi, n_sources=4, seed=3),
+                  OP.Helmholtz2D, None, 3),
+}
+
+
+def _points(recipe, n, seed):
+    rng = np.random.default_rng(seed)
+    if recipe == "ho_hardbc":
+        return rng.uniform(0, 1, (n, 1)).astype(np.float32)
+    if recipe == "burgers":
+        return np.stack([rng.uniform(-1, 1, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
+    if recipe == "wave":
+        return np.stack([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
+    return rng.uniform(0, 1, (n, 2)).astype(np.float32)
+
+
+def _required(name):
+    return {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))), "burgers": ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0))),
+            "poisson": ((0, (0, 0)), (0, (1, 1))), "wave": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2))),
+            "helmholtz": ((0, ()), (0, (0, 0)), (0, (1, 1)))}[name]
+
+
+def _oracle_loss_grad(name, static, layers64, x, prob_static):
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    if opar is None:
+        opar = {"sd": prob_static["sd"], "k": prob_static["k"], "source": prob_static["source"].double()}
+    P = oracle_params(static, layers64, opar)
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(static["m"], dtype=int), p[0].numpy(),
+                                                          p[1].numpy(), static["subdomain"]["pou"].numpy())
+    loss, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
+                                       [OM.get_jmaps(_required(name))], ocls)
+    gpack = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
+    return loss.item(), gpack, a_ims, active
+
+
+@pytest.mark.parametrize("name", ["ho_hardbc", "burgers", "poisson", "wave", "helmholtz"])
+def test_fused_loss_and_gradient_vs_oracle(cuda, name):
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    static = decomposition(recipe)
+    layers64 = random_layers(ls, static["m"], seed=5)
+    layers32 = [(w.float().double(), b.float().double()) for w, b in layers64]
+    x = _points(recipe if recipe != "multilevel" else "poisson", 600, 17)
+    prob_static = pcls.init_params(**pkw)[0]
+    loss_ref, g_ref, a_ims, active = _oracle_loss_grad(name, static, layers32, x, prob_static)
+    assert d2mask_of([_required(name)], x.shape[1]) | d2 == d2
+    eng = _engine(static, layers32, d2)
+    eng.set_state(active)
+    eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+    ps = eng.points(torch.tensor(x))
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    assert abs(loss - loss_ref) <= JET_TOL * abs(loss_ref), (loss, loss_ref)
+    assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
+    inactive = np.setdiff1d(np.arange(static["m"]), a_ims)
+    assert np.all(grad[inactive] == 0)
+
+
+def test_generic_path_matches_fused(cuda):
+    """FBPINNJet + constrained_jets + loss_fn in torch == the fused kernel path."""
+    name = "burgers"
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    static = decomposition(recipe)
+    layers = random_layers(ls, static["m"], seed=9)
+    x = torch.tensor(_points(recipe, 500, 4))
+    eng = _engine(static, layers, d2)
+    prob_static = pcls.init_params(**pkw)[0]
+    all_params = {"static": {"problem": prob_static}, "trainable": {}}
+    eng.set_problem(pcls.fused_spec(all_params))
+    ps = eng.points(x)
+    eng.forward_pairs(ps)
+    loss_f = eng.pou_loss(ps).item()
+    grad_f = eng.adjoint(ps).clone()
+    theta = eng.theta.clone().requires_grad_(True)
+    U = FBPINNJet.apply(theta, eng, ps)
+    xc = ps.x
+    Uc = constrained_jets(pcls.constraining_fn, all_params, xc, U, 2, d2)
+    ujs = [Uc[:, jet_index(2, d2, ixs):jet_index(2, d2, ixs) + 1] for _, ixs in _required(name)]
+    loss_g = pcls.loss_fn(all_params, [[xc] + ujs])
+    loss_g.backward()
+    assert abs(loss_g.item() - loss_f) <= 1e-5 * abs(loss_f)
+    assert rel_err(theta.grad.cpu().numpy(), grad_f.cpu().numpy()) < GRAD_TOL
+
+
+def test_generic_two_constraints_and_inverse_vs_oracle(cuda):
+    """Soft-BC oscillator (two constraints, one with a single point) and the
+    inverse problem's trainable mu, through the generic path."""
+    from fbpinns_gb300.trainers import GenericStep
+    static = decomposition("ho")
+    layers = random_layers([1, 16, 16, 1], static["m"], seed=2)
+    for pcls, ocls, pkw in [(PR.HarmonicOscillator1D, OP.HarmonicOscillator1D, dict(d=2, w0=20)),
+                            (PR.HarmonicOscillator1DInverse, OP.HarmonicOscillator1DInverse, dict(d=2, w0=20))]:
+        ps_, pt_ = pcls.init_params(**pkw)
+        all_params = {"static": {"problem": ps_, "decomposition": static},
+                      "trainable": {"problem": {k: v.clone().float().cuda() for k, v in pt_.items()}}}
+        from fbpinns_gb300.domains import RectangularDomainND
+        dom_ps = RectangularDomainND.init_params(np.array([0.]), np.array([1.]))[0]
+        all_params["static"]["domain"] = dom_ps
+        cons = pcls.sample_constraints(all_params, RectangularDomainND, 0, "grid", ((50,),))
+        eng = FBPINNEngine(static, [1, 16, 16, 1], d2mask_of([c[-1] for c in cons], 1), chunk=64)
+        eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+        step = GenericStep(eng, pcls, all_params, [c[:-1] for c in cons], [c[-1] for c in cons])
+        theta = eng.theta.clone().requires_grad_(True)
+        loss, gtheta, gprob = step.loss_and_grads(theta)
+        # oracle
+        x_all = np.concatenate([c[0].numpy() for c in cons]).astype(np.float32)
+        offs = np.cumsum([0] + [c[0].shape[0] for c in cons[:-1]])
+        cf = np.zeros((x_all.shape[0], len(cons)), bool)
+        for ic, c in enumerate(cons):
+            cf[offs[ic]:offs[ic] + c[0].shape[0], ic] = True
+        p = static["subdomain"]["params"]
+        takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x_all, np.ones(static["m"], dtype=int), p[0].numpy(),
+                                                              p[1].numpy(), static["subdomain"]["pou"].numpy())
+        takess = OT.split_takes(takes, cf, x_all.shape[0])
+        ocons = [[torch.tensor(c[0].numpy(), dtype=torch.float64)] + [torch.as_tensor(v).double() for v in c[1:-1]]
+                 for c in cons]
+        layers32 = [(w.float().double(), b.float().double()) for w, b in layers]
+        P = oracle_params(static, layers32, {k: (v if not torch.is_tensor(v) else v.double()) for k, v in ps_.items()
+                                             if k != "c_fn"})
+        P["problem_trainable"] = {k: v.double() for k, v in pt_.items()}
+        lref, gref, gpr = OM.value_and_grad(P, a_ims, f_ims, ocons, takess, [OM.get_jmaps(c[-1]) for c in cons], ocls,
+                                            trainable_problem_keys=tuple(pt_.keys()))
+        assert abs(loss.item() - lref.item()) <= 1e-5 * abs(lref.item()), (pcls.__name__, loss.item(), lref.item())
+        gpack = torch.cat([t.reshape(len(a_ims), -1) for dw, db in gref for t in (dw, db)], 1).numpy()
+        assert rel_err(gtheta.cpu().numpy()[a_ims], gpack) < GRAD_TOL, pcls.__name__
+        for k in pt_:
+            assert abs(gprob[k].item() - gpr[k].item()) <= 1e-4 * max(abs(gpr[k].item()), 1e-6)
+
+
+def test_adam_matches_optax_semantics(cuda):
+    static = decomposition("ho")
+    eng = FBPINNEngine(static, [1, 8, 8, 1], d2mask=1)
+    m, P = eng.m, eng.P
+    g = torch.Generator().manual_seed(0)
+    theta0 = torch.randn((m, P), generator=g)
+    eng.set_theta(theta0)
+    state = np.ones(m, dtype=int)
+    state[3] = 2
+    state[5] = 0
+    eng.set_state(state)
+    th, mu, nu, cnt = theta0.double(), torch.zeros(m, P, dtype=torch.float64), torch.zeros(m, P, dtype=torch.float64), 0
+    for it in range(3):
+        grad = torch.randn((m, P), generator=g)
+        eng.adam(1e-3, grad=grad.cuda())
+        mask = torch.tensor(state == 1)[:, None]
+        th2, mu2, nu2, cnt2 = OM.adam_update(th, grad.double(), mu, nu, cnt, 1e-3)
+        th = torch.where(mask, th2, th)
+        mu = torch.where(mask, mu2, mu)
+        nu = torch.where(mask, nu2, nu)
+        cnt = cnt2
+    assert int(eng.count.item()) == 3
+    got = eng.theta.cpu().double()
+    assert torch.equal(got[3], theta0[3].double()) and torch.equal(got[5], theta0[5].double())
+    assert (got - th).abs().max().item() < 1e-6

@@ -1,0 +1,138 @@
+"""Interaction lists on the GPU: bit-exact against the reference's golden
+vectors and against the oracle, including edge cases and full-size runs."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from helpers import decomposition, boxes_static
+from oracle import takes as OT
+from fbpinns_gb300 import takes as T
+from fbpinns_gb300.engine import FBPINNEngine
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.cpu().numpy().astype(np.int64)
+
+
+def test_kat_inside_points_and_models(cuda):
+    """decompositions_base.py:87-128 known-answer configuration (seeded points)."""
+    g = golden("takes_kat.npz")
+    st = boxes_static(g["xmin"], g["xmax"])
+    n_take, m_take, iims = T.inside_points(st, torch.tensor(g["x"]))
+    np.testing.assert_array_equal(_np(n_take), g["n_take"])
+    np.testing.assert_array_equal(_np(m_take), g["m_take"])
+    np.testing.assert_array_equal(_np(iims), g["inside_ims"])
+    ips, d = T.inside_models(st, torch.tensor(g["x"]), np.arange(1000))
+    np.testing.assert_array_equal(_np(ips), g["inside_ips"])
+    assert abs(d - float(g["d"])) <= 1e-6 * abs(float(g["d"]))
+
+
+@pytest.mark.parametrize("tag", ["ho", "ho2c", "burgers_all", "burgers_sched", "multilevel", "wave3d"])
+def test_get_inputs_bit_exact(cuda, tag):
+    """get_inputs + _get_x_batch + per-constraint split (trainers.py:332-575)."""
+    g = golden(f"inputs_{tag}.npz")
+    static = decomposition(tag)
+    all_params = {"static": {"decomposition": static}}
+    ims = np.arange(static["m"])[g["active_in"] == 1]
+    ips, _ = T.inside_models(static, torch.tensor(g["x_global"]), ims)
+    x_batch = g["x_global"][_np(ips)]
+    np.testing.assert_array_equal(x_batch, g["x_batch"])
+    takes, all_ims, (active, _, _) = T.get_inputs(x_batch, g["active_in"], all_params)
+    np.testing.assert_array_equal(active, g["active_out"])
+    np.testing.assert_array_equal(_np(all_ims), g["all_ims"])
+    for k, nm in enumerate(["m_take", "n_take", "p_take", "np_take"]):
+        np.testing.assert_array_equal(_np(takes[k]), g[nm])
+    assert takes[4] == int(g["npou"])
+    cfs = g["constraint_fs"][_np(ips)]
+    offsets = [int(cfs[:, :ic].any(1).sum()) if ic else 0 for ic in range(cfs.shape[1])]
+    for ic, tk in enumerate(T.split_takes(takes, offsets, x_batch.shape[0])):
+        for k, nm in enumerate(["m_take", "n_take", "p_take", "np_take"]):
+            np.testing.assert_array_equal(_np(tk[k]), g[f"c{ic}_{nm}"])
+
+
+def _oracle_takes(static, x):
+    p = static["subdomain"]["params"]
+    xmins, xmaxs = p[0].numpy(), p[1].numpy()
+    pou = static["subdomain"]["pou"].numpy()
+    takes, all_ims, _ = OT.get_inputs(x, np.ones(static["m"], dtype=int), xmins, xmaxs, pou)
+    return takes
+
+
+@pytest.mark.parametrize("n,seed", [(1, 0), (7, 1), (4097, 2), (60000, 3)])
+def test_random_points_multilevel_vs_oracle(cuda, n, seed):
+    static = decomposition("multilevel")
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-0.05, 1.05, (n, 2)).astype(np.float32)  # some points outside every box
+    x[: min(n, 3)] = np.float32(0.5)                          # duplicates on box edges/centres
+    ref = _oracle_takes(static, x)
+    takes, _, _ = T.get_inputs(x, np.ones(static["m"], dtype=int), {"static": {"decomposition": static}})
+    for k in range(4):
+        np.testing.assert_array_equal(_np(takes[k]), ref[k])
+
+
+def test_points_on_box_boundaries_3d(cuda):
+    """Points exactly on box faces (closed boxes) and outside the decomposition."""
+    static = decomposition("wave")
+    p = static["subdomain"]["params"]
+    corners = torch.cat([p[0], p[1]]).numpy()
+    x = np.concatenate([corners, corners + np.float32(1e-7), corners - np.float32(1e-7),
+                        np.array([[5., 5., 5.], [-5., 0., 0.5]], np.float32)]).astype(np.float32)
+    ref = _oracle_takes(static, x)
+    takes, _, _ = T.get_inputs(x, np.ones(static["m"], dtype=int), {"static": {"decomposition": static}})
+    for k in range(4):
+        np.testing.assert_array_equal(_np(takes[k]), ref[k])
+
+
+def test_sort_and_work_queue(cuda):
+    """The subdomain-major order is a stable sort of the pairs by subdomain and the
+    work items tile each subdomain's run."""
+    static = decomposition("poisson")
+    eng = FBPINNEngine(static, [2, 16, 16, 1], d2mask=3, chunk=256)
+    rng = np.random.default_rng(7)
+    x = torch.tensor(rng.uniform(0, 1, (20000, 2)).astype(np.float32))
+    ps = eng.points(x)
+    s = ps.s
+    m_take = _np(ps.takes.m_take[:s])
+    order = np.argsort(m_take, kind="stable")
+    np.testing.assert_array_equal(_np(ps.sd_pair[:s]), order)
+    np.testing.assert_array_equal(_np(ps.sd_point[:s]), _np(ps.takes.n_take[:s])[order])
+    np.testing.assert_array_equal(_np(ps.sd_slot[:s]), _np(ps.takes.p_take[:s])[order])
+    counts = np.bincount(m_take, minlength=static["m"])
+    np.testing.assert_array_equal(_np(ps.sd_start), np.concatenate([[0], np.cumsum(counts)]))
+    nit = int(ps.n_items_all.item())
+    items = _np(ps.items_all[: 3 * nit]).reshape(-1, 3)
+    cover = np.zeros(s, dtype=np.int64)
+    for j, b, c in items:
+        assert 0 < c <= 256
+        assert m_take[order[b:b + c]].tolist() == [j] * c
+        cover[b:b + c] += 1
+    assert (cover == 1).all()
+
+
+@pytest.mark.slow
+def test_full_size_poisson_takes(cuda):
+    """2D multilevel Poisson at full size (2^18 uniform points, 1365 boxes):
+    bit-exact against the oracle's dense point-in-box test."""
+    static = decomposition("poisson")
+    rng = np.random.default_rng(11)
+    x = rng.uniform(0, 1, (1 << 18, 2)).astype(np.float32)
+    takes, _, _ = T.get_inputs(x, np.ones(static["m"], dtype=int), {"static": {"decomposition": static}})
+    p = static["subdomain"]["params"]
+    xmins, xmaxs = p[0].numpy(), p[1].numpy()
+    n_ref, m_ref = [], []
+    for i in range(0, x.shape[0], 8192):
+        a, b = np.nonzero(OT.inside_rectangle(xmins, xmaxs, x[i:i + 8192], np.arange(static["m"])))
+        n_ref.append(a + i)
+        m_ref.append(b)
+    np.testing.assert_array_equal(_np(takes[1]), np.concatenate(n_ref))
+    np.testing.assert_array_equal(_np(takes[0]), np.concatenate(m_ref))
+    # slots: np_take sorted, p_take consistent with (point, level)
+    pou = static["subdomain"]["pou"].numpy().reshape(-1).astype(np.int64)
+    key = np.concatenate(n_ref) * 64 + pou[np.concatenate(m_ref)]
+    u, inv = np.unique(key, return_inverse=True)
+    np.testing.assert_array_equal(_np(takes[2]), inv)
+    np.testing.assert_array_equal(_np(takes[3]), u // 64)
