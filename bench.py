@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""FBPINN train steps/s on one GB300: fused CUDA step vs the plain GPU step.
+
+Workload (the 2D multilevel Poisson configuration): -lap u = f on [0,1]^2,
+u = sum_{k=1..6} sin(2^k pi x) sin(2^k pi y) / 2^k, hard zero BC; multilevel
+rectangular decomposition with 1, 2^2, 4^2, 8^2, 16^2, 32^2 subdomains
+(m = 1365, width 2.9 x spacing, the single level-1 box [0,1]^2); FCN 2-16-16-1
+tanh per subdomain; 2^18 uniform collocation points redrawn on the device every
+step; Adam lr 1e-3.  A step = sample + interaction lists + sort + work queues +
+forward jets + POU/residual/FP64 loss + adjoint + gradient reduce + Adam, one
+CUDA graph.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fused|reference]
+Under torchrun (N > 1) every rank runs an independent replica (the step does
+not shard across GPUs); value = steps/s summed over ranks, timed by the
+slowest rank.  Prints one JSON line on rank 0.
+"""
+
+import argparse
+import csv
+import io
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_POINTS = 1 << 18
+LAYERS = [2, 16, 16, 1]
+LEVELS = [1, 2, 4, 8, 16, 32]
+WIDTH = 2.9
+LR = 1e-3
+SEED = 0
+METRIC = "FBPINN train steps/s, fused adjoint vs plain GPU step, at matched test L1 error"
+WORKLOAD = "poisson2d_multilevel_m1365_fcn2-16-16-1_n262144_resampled"
+
+
+def decomposition_static():
+    from fbpinns_gb300.constants import get_subdomain_ws
+    from fbpinns_gb300.decompositions import MultilevelRectangularDecompositionND
+    sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in LEVELS[1:]]
+    sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, WIDTH) for s in sxs[1:]]
+    return MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
+
+
+def init_theta(m, seed=SEED):
+    from fbpinns_gb300.networks import FCN, pack_layers
+    from fbpinns_gb300.trainers import init_subdomain_networks
+    _, tr = init_subdomain_networks(FCN, {"layer_sizes": LAYERS}, m, seed)
+    return pack_layers(tr["layers"])
+
+
+def problem_setup():
+    from fbpinns_gb300.problems import Poisson2D
+    ps = Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    return Poisson2D, {"static": {"problem": ps}, "trainable": {}}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restatement of the reference step, FP32, all threads)
+# ---------------------------------------------------------------------------
+class CPUReferenceStep:
+    """One step of the reference algorithm on the host cores: the oracle's
+    restatement (per-pair parameter gathers, nested forward-mode jets, reverse-mode
+    gradient, Adam) in FP32 torch-CPU on ``n_sample`` fresh uniform points."""
+
+    def __init__(self, static, theta_cpu, n_sample, threads):
+        from oracle import model as OM
+        from fbpinns_gb300.networks import unpack_layers
+        torch.set_num_threads(threads)
+        self.OM = OM
+        self.static, self.n_sample = static, n_sample
+        p = static["subdomain"]["params"]
+        self.layers = [(w.clone(), b.clone()) for w, b in unpack_layers(theta_cpu.clone().float(), LAYERS)]
+        self.P = {"xmins": p[0].float(), "xmaxs": p[1].float(), "flags": p[4].float(), "unnorms": p[5].float(),
+                  "pou": static["subdomain"]["pou"].float(), "layers": self.layers,
+                  "problem": {"sd": 0.1, "n_freq": 6}, "problem_trainable": {}}
+        self.mu = [torch.zeros_like(t) for wb in self.layers for t in wb]
+        self.nu = [torch.zeros_like(t) for wb in self.layers for t in wb]
+        self.jm = OM.get_jmaps(((0, (0, 0)), (0, (1, 1))))
+        self.rng = np.random.default_rng(1)
+        self.count = 0
+
+    def step(self):
+        from oracle import problems as OP
+        from oracle import takes as OT
+        OM, st, P = self.OM, self.static, self.P
+        p = st["subdomain"]["params"]
+        x = self.rng.uniform(0, 1, (self.n_sample, 2)).astype(np.float32)
+        t0 = time.perf_counter()
+        takes, all_ims, (act, a_ims, f_ims) = OT.get_inputs(x, np.ones(st["m"], dtype=int), p[0].numpy(),
+                                                           p[1].numpy(), st["subdomain"]["pou"].numpy())
+        loss, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x)]], [takes], [self.jm], OP.Poisson2D)
+        ai = torch.as_tensor(a_ims, dtype=torch.long)
+        flat = [t for gw in grads for t in gw]
+        for li, (w, b) in enumerate(P["layers"]):
+            for k, t in enumerate((w, b)):
+                idx = 2 * li + k
+                g = torch.zeros_like(t)
+                g[ai] = flat[idx].to(t.dtype)
+                th, self.mu[idx], self.nu[idx], _ = OM.adam_update(t, g, self.mu[idx], self.nu[idx], self.count, LR)
+                t.copy_(th)
+        self.count += 1
+        return time.perf_counter() - t0
+
+
+def cpu_baseline(static, theta_cpu, threads, n_sample=1024, budget_s=10.0):
+    """Median seconds per CPU reference step over ~budget_s of work."""
+    ref = CPUReferenceStep(static, theta_cpu, n_sample, threads)
+    ref.step()
+    times, t_end = [], time.time() + budget_s
+    while len(times) < 2 or (time.time() < t_end and len(times) < 50):
+        times.append(ref.step())
+    return float(np.median(times)), len(times)
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    static = decomposition_static()
+    theta = init_theta(static["m"])
+    threads = os.cpu_count() or 1
+    n_sample = 1024
+    ref = CPUReferenceStep(static, theta, n_sample, threads)
+    for _ in range(args.warmup):
+        ref.step()
+    t0 = time.perf_counter()
+    per_step = [ref.step() for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
+    t_step = wall / args.steps
+    value = (n_sample / N_POINTS) / t_step  # full-workload steps/s: pairs scale linearly with points
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points)",
+            "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "sample_points": n_sample},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_sample} of {N_POINTS} uniform points per step on the full decomposition "
+                                       f"(oracle restatement, FP32 torch-CPU); steps/s scaled by "
+                                       f"{n_sample}/{N_POINTS}; median step {1000 * float(np.median(per_step)):.1f} ms"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_fused(args, world, rank, local):
+    from fbpinns_gb300 import _lib
+    from fbpinns_gb300.engine import FBPINNEngine
+    from fbpinns_gb300.optim import adam
+    from fbpinns_gb300.plain import PlainStep
+    from fbpinns_gb300.trainers import FusedStep
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    static = decomposition_static()
+    problem, all_params = problem_setup()
+    spec = problem.fused_spec(all_params)
+    theta0 = init_theta(static["m"])
+    opt = adam(LR)
+    seed = SEED + 1000 * rank
+
+    eng = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid)
+    eng.set_theta(theta0)
+    step = FusedStep(eng, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
+    for _ in range(max(args.warmup, 3)):
+        step.step()
+    torch.cuda.synchronize()
+    pairs = int(step.ps.takes.pt_off[N_POINTS].item())
+    slots = int(step.ps.takes.np_off[N_POINTS].item())
+
+    clk = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step.step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_max = max_over_ranks(ms, world)
+    step.check()
+    loss_last = float(eng.loss.item())
+    value = world * 1000.0 / ms_max
+
+    # ---- end to end through the public step API with host buffers ----------
+    e2e = None
+    try:
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid)
+        eng2.set_theta(theta0)
+        rng = np.random.default_rng(seed + 7)
+        nh = 4
+        host = [torch.from_numpy(rng.uniform(0, 1, (N_POINTS, 2)).astype(np.float32)).pin_memory() for _ in range(nh)]
+        hstep = FusedStep(eng2, spec, opt, host_points=N_POINTS, x_probe=host[0], use_graph=True)
+        for k in range(max(args.warmup, 3)):
+            hstep.step(host[k % nh])
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for k in range(args.steps):
+            hstep.step(host[k % nh])
+        f1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier(world)
+        ms_e = max(f0.elapsed_time(f1), 1000 * wall) / args.steps
+        ms_e = max_over_ranks(ms_e, world)
+        hstep.check()
+        e2e = {"value": world * 1000.0 / ms_e, "unit": "steps/s", "h2d_bytes_per_step": N_POINTS * 2 * 4,
+               "d2h_bytes_per_step": 8}
+        del hstep, eng2
+    except Exception as ex:  # reported, not hidden
+        e2e = {"value": None, "unit": "steps/s", "error": repr(ex)[:200]}
+
+    # ---- per-kernel timing (eager, CUDA events on the launching stream) ----
+    ps = step.ps
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    reps = 5
+    timings = {}
+
+    def timed(name, fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        timings[name] = a.elapsed_time(b) / reps
+
+    timed("takes_sort_work", lambda: ps.rebuild())
+    timed("forward_pairs", lambda: eng.forward_pairs(ps))
+    timed("pou_loss", lambda: eng.pou_loss(ps))
+    timed("adjoint_pairs", lambda: eng.adjoint(ps, reduce=False))
+    timed("grad_reduce", lambda: eng.reduce_grad(ps))
+    timed("adam", lambda: eng.adam(0.0))
+    sig = float(sum(a * b for a, b in zip(LAYERS[:-1], LAYERS[1:])))
+    J = eng.J
+    fl_fwd = pairs * 2 * J * sig
+    fl_adj = pairs * 4 * J * sig
+    # FP32 FMA throughput probe (roofline denominator)
+    sink = torch.zeros(256, device=dev)
+    import ctypes as C
+    flops = C.c_double()
+    best = 0.0
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    for _ in range(3):
+        a, b = ev(), ev()
+        a.record()
+        _lib.check(lib.fbp_fma_probe(_lib.ptr(sink), sms * 8, 8192, C.byref(flops), _lib.stream_ptr()))
+        b.record()
+        torch.cuda.synchronize()
+        best = max(best, flops.value / (a.elapsed_time(b) * 1e-3) / 1e12)
+    dom = max(("forward_pairs", "adjoint_pairs"), key=lambda k: timings[k])
+    ach = (fl_adj if dom == "adjoint_pairs" else fl_fwd) / (timings[dom] * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": best, "unit": "TFLOP/s", "frac": ach / best,
+                "peak_source": "FP32 FMA probe (fbp_fma_probe) measured in this run; MEASURED_PEAKS.json has no FP32 figure",
+                "traffic": None,
+                "kernel_ms": {k: round(v, 4) for k, v in timings.items()},
+                "algorithmic_flops_per_launch": {"forward_pairs": fl_fwd, "adjoint_pairs": fl_adj}}
+
+    # ---- plain GPU step (torch autograd) ----
+    plain = None
+    if not args.no_plain:
+        try:
+            eng3 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk)
+            eng3.set_theta(theta0)
+            pstep = PlainStep(eng3, problem, all_params, ((0, (0, 0)), (0, (1, 1))), opt,
+                              resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed))
+            for _ in range(2):
+                pstep.step()
+            torch.cuda.synchronize()
+            kp = max(3, min(args.steps, 10))
+            a, b = ev(), ev()
+            a.record()
+            for _ in range(kp):
+                pstep.step()
+            b.record()
+            torch.cuda.synchronize()
+            ms_p = max_over_ranks(a.elapsed_time(b) / kp, world)
+            plain = {"value": world * 1000.0 / ms_p, "unit": "steps/s", "ms_per_step": ms_p, "steps": kp,
+                     "fused_over_plain": ms_p / ms_max}
+            del pstep, eng3
+        except Exception as ex:
+            plain = {"value": None, "error": repr(ex)[:300]}
+        torch.cuda.empty_cache()
+
+    # ---- CPU baseline (rank 0 only) ----
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        n_sample = 1024
+        t_cpu, nsteps = cpu_baseline(static, theta0.cpu(), threads, n_sample)
+        cpu = {"value": (n_sample / N_POINTS) / t_cpu, "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": f"{nsteps} steps of {n_sample} of {N_POINTS} uniform points on the full decomposition "
+                         f"(oracle restatement in FP32 torch-CPU); steps/s scaled by {n_sample}/{N_POINTS}"}
+
+    # launches of our kernels in one step (counted from the C-ABI calls of the step body)
+    per_step = (1 + 1 + 3 + 3 + 1 + 6 + 5 + 5 + 1 + 1 + 1 + 1 + 1 + 2)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
+                "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
+                           "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
+                           "parallelism": f"replicas x{world}", "chunk": args.chunk,
+                           "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
+                                 ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
+                "e2e": e2e, "gpu_launches": per_step * args.steps, "clocks": clocks, "roofline": roofline,
+                "cpu_baseline": cpu, "plain": plain, "loss_last": loss_last,
+                "evals_per_s": value * pairs}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
+    ap.add_argument("--chunk", type=int, default=512)
+    ap.add_argument("--grid", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_fused(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -302,16 +302,23 @@ class FBPINNEngine:
                                          _lib.ptr(self.loss), st), "fbp_loss_finalize")
         return self.loss
 
-    def adjoint(self, ps, theta=None, out=None, stream=None):
+    def adjoint(self, ps, theta=None, out=None, stream=None, reduce=True):
         lib = _lib.load()
         st = _lib.stream_ptr(stream)
         net = self.net_struct(theta)
         pr = ps.pairs_struct(True)
         _lib.check(lib.fbp_adjoint_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
                                          _lib.ptr(ps.grad_part), self.launch_grid, st), "fbp_adjoint_pairs")
+        if not reduce:
+            return None
+        return self.reduce_grad(ps, out, stream)
+
+    def reduce_grad(self, ps, out=None, stream=None):
+        """grad[j] = sum of subdomain j's work-item partials, in item order."""
+        lib = _lib.load()
         out = self.grad if out is None else out
         _lib.check(lib.fbp_grad_reduce(_lib.ptr(ps.grad_part), _lib.ptr(ps.item_start_act), self.m, self.P,
-                                       _lib.ptr(out), st), "fbp_grad_reduce")
+                                       _lib.ptr(out), _lib.stream_ptr(stream)), "fbp_grad_reduce")
         return out
 
     def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8, eps_root=0.0, grad=None, stream=None):

@@ -112,8 +112,7 @@ class PointTakes:
         b = self.grid.boxes(select)
         assert x.is_cuda and x.dtype == torch.float32 and x.shape == (self.n, self.grid.xd)
         x = x.contiguous()
-        self.model_count.zero_()
-        self.status.zero_()
+        self.model_count.zero_()  # the status word is sticky: cleared only by reset_status()
         _lib.check(lib.fbp_inside_count(_lib.ptr(x), self.n, C.byref(b), _lib.ptr(self.pt_count),
                                         _lib.ptr(self.pt_nlvl), _lib.ptr(self.pt_lvl), _lib.ptr(self.model_count),
                                         st), "fbp_inside_count")
@@ -141,6 +140,9 @@ class PointTakes:
     def sizes(self):
         """(s, u) read back from the device."""
         return int(self.pt_off[self.n].item()), int(self.np_off[self.n].item())
+
+    def reset_status(self):
+        self.status.zero_()
 
     def check_status(self):
         w = int(self.status.item())

@@ -107,44 +107,55 @@ class GenericStep:
 class FusedStep:
     """The fused CUDA step for a built-in problem.
 
-    ``x`` fixes the collocation points; alternatively ``resample=(n, xmin,
-    xmax, seed)`` draws n new uniform points on the device every step (offset
-    by the device step count) and rebuilds the interaction lists into
-    fixed-capacity buffers, so the whole step has no host synchronisation and
-    is captured in a CUDA graph when ``use_graph``.
+    Point modes:
+      ``x=...``          fixed collocation points (exact buffer sizes);
+      ``resample=(n, xmin, xmax, seed)``  n new uniform points drawn on the
+                         device every step (stream offset = device step count);
+      ``host_points=n``  the caller passes each step's points from (pinned)
+                         host memory to ``step(x_host)``.
+    In the last two modes the interaction lists are rebuilt every step into
+    fixed-capacity buffers (``headroom`` x the first batch's sizes), so the step
+    has no host synchronisation and is captured in one CUDA graph when
+    ``use_graph``.
     """
 
-    def __init__(self, engine, spec, opt, x=None, resample=None, use_graph=True, headroom=1.25):
+    def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
+                 headroom=1.25):
         self.eng, self.opt = engine, opt
         engine.set_problem(spec)
         self.resample = resample
+        self.host = host_points is not None
         self.use_graph = use_graph
         self.graph = None
-        self.h2d_src = None
-        if resample is not None:
-            n, xmin, xmax, seed = resample
-            self.xmin, self.xmax, self.seed = list(xmin), list(xmax), int(seed)
-            x0 = torch.empty((n, engine.xd), dtype=torch.float32, device=engine.device)
-            engine.sample(x0, self.seed, 1 << 32, self.xmin, self.xmax)
+        dev = engine.device
+        if resample is not None or self.host:
+            if resample is not None:
+                n, xmin, xmax, seed = resample
+                self.xmin, self.xmax, self.seed = list(xmin), list(xmax), int(seed)
+                x0 = torch.empty((n, engine.xd), dtype=torch.float32, device=dev)
+                engine.sample(x0, self.seed, 1 << 32, self.xmin, self.xmax)
+            else:
+                x0 = torch.as_tensor(x_probe, dtype=torch.float32).to(dev)
+                assert x0.shape[0] == host_points
             probe = engine.points(x0)
-            s, u = probe.s, probe.u
-            caps = (int(s * headroom) + 1024, int(u * headroom) + 1024)
+            caps = (int(probe.s * headroom) + 1024, int(probe.u * headroom) + 1024)
             del probe
             self.ps = engine.points(x0, caps=caps)
         else:
-            self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(engine.device))
+            self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(dev))
+        self.loss_host = torch.zeros(1, dtype=torch.float64, pin_memory=True)
 
     def set_state(self, active):
         self.eng.set_state(active)
         self.ps.build_work()
+        self.graph = None
 
     def _body(self, stream=None):
         eng, o = self.eng, self.opt
         if self.resample is not None:
             eng.sample(self.ps.x, self.seed, 0, self.xmin, self.xmax, counter=eng.count, stream=stream)
             self.ps.rebuild(stream=stream)
-        elif self.h2d_src is not None:
-            self.ps.x.copy_(self.h2d_src, non_blocking=True)
+        elif self.host:
             self.ps.rebuild(stream=stream)
         return eng.fused_step(self.ps, o["learning_rate"], stream=stream, b1=o["b1"], b2=o["b2"], eps=o["eps"],
                               eps_root=o["eps_root"])
@@ -162,13 +173,20 @@ class FusedStep:
             self._body()
         self.graph = g
 
-    def step(self):
+    def step(self, x_host=None):
+        """One training step; returns the device loss.  In host mode x_host
+        (n, xd) float32, ideally pinned, is copied in first and the loss is
+        copied back to ``loss_host`` (read it after a synchronisation)."""
+        if self.host:
+            self.ps.x.copy_(x_host, non_blocking=True)
         if self.use_graph:
             if self.graph is None:
                 self.capture()
             self.graph.replay()
         else:
             self._body()
+        if self.host:
+            self.loss_host.copy_(self.eng.loss, non_blocking=True)
         return self.eng.loss
 
     def check(self):

@@ -156,7 +156,7 @@ def test_generic_two_constraints_and_inverse_vs_oracle(cuda):
     inverse problem's trainable mu, through the generic path."""
     from fbpinns_gb300.trainers import GenericStep
     static = decomposition("ho")
-    layers = random_layers([1, 16, 16, 1], static["m"], seed=2)
+    layers = random_layers([1, 8, 8, 1], static["m"], seed=2)
     for pcls, ocls, pkw in [(PR.HarmonicOscillator1D, OP.HarmonicOscillator1D, dict(d=2, w0=20)),
                             (PR.HarmonicOscillator1DInverse, OP.HarmonicOscillator1DInverse, dict(d=2, w0=20))]:
         ps_, pt_ = pcls.init_params(**pkw)
@@ -166,7 +166,7 @@ def test_generic_two_constraints_and_inverse_vs_oracle(cuda):
         dom_ps = RectangularDomainND.init_params(np.array([0.]), np.array([1.]))[0]
         all_params["static"]["domain"] = dom_ps
         cons = pcls.sample_constraints(all_params, RectangularDomainND, 0, "grid", ((50,),))
-        eng = FBPINNEngine(static, [1, 16, 16, 1], d2mask_of([c[-1] for c in cons], 1), chunk=64)
+        eng = FBPINNEngine(static, [1, 8, 8, 1], d2mask_of([c[-1] for c in cons], 1), chunk=64)
         eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
         step = GenericStep(eng, pcls, all_params, [c[:-1] for c in cons], [c[-1] for c in cons])
         theta = eng.theta.clone().requires_grad_(True)
@@ -221,3 +221,142 @@ def test_adam_matches_optax_semantics(cuda):
     got = eng.theta.cpu().double()
     assert torch.equal(got[3], theta0[3].double()) and torch.equal(got[5], theta0[5].double())
     assert (got - th).abs().max().item() < 1e-6
+
+
+def test_plain_step_matches_fused(cuda):
+    """The plain torch-autograd drop-in step computes the same loss and gradient."""
+    from fbpinns_gb300.plain import PlainStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("multilevel")
+    layers = random_layers([2, 8, 8, 1], static["m"], seed=4)
+    x = torch.tensor(_points("poisson", 1500, 8))
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    all_params = {"static": {"problem": prob_static}, "trainable": {}}
+    eng = _engine(static, layers, 3)
+    eng.set_problem(PR.Poisson2D.fused_spec(all_params))
+    ps = eng.points(x)
+    eng.forward_pairs(ps)
+    loss_f = eng.pou_loss(ps).item()
+    grad_f = eng.adjoint(ps).cpu().numpy()
+    pstep = PlainStep(eng, PR.Poisson2D, all_params, _required("poisson"), adam(1e-3), x=x)
+    theta = eng.theta.detach().clone().requires_grad_(True)
+    loss_p = pstep.loss(theta)
+    (g,) = torch.autograd.grad(loss_p, [theta])
+    assert abs(loss_p.item() - loss_f) <= 1e-5 * abs(loss_f)
+    assert rel_err(g.cpu().numpy(), grad_f) < GRAD_TOL
+
+
+def test_resampled_graph_step_is_deterministic_and_matches_eager(cuda):
+    """Device resampling + interaction lists + fused step captured in a CUDA graph
+    gives bit-identical parameters to the same steps run eagerly."""
+    from fbpinns_gb300.trainers import FusedStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=1)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    results = []
+    for use_graph, calls in ((True, 4), (False, 6)):  # capture runs 2 eager warm-up steps first
+        eng = _engine(static, layers, 3, chunk=512)
+        st = FusedStep(eng, spec, adam(1e-3), resample=(1 << 14, [0., 0.], [1., 1.], 3), use_graph=use_graph)
+        for _ in range(calls):
+            loss = st.step()
+        torch.cuda.synchronize()
+        st.check()
+        results.append((eng.theta.cpu().clone(), loss.item(), int(eng.count.item())))
+    (t_g, l_g, c_g), (t_e, l_e, c_e) = results
+    assert c_g == c_e == 6
+    assert np.isfinite(l_g) and l_g == l_e
+    assert torch.equal(t_g, t_e)
+
+
+def test_resampled_steps_match_oracle_points(cuda):
+    """The points drawn on the device are uniform in the box and each step's
+    interaction lists equal the oracle's for those points."""
+    from fbpinns_gb300.trainers import FusedStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("multilevel")
+    layers = random_layers([2, 8, 8, 1], static["m"], seed=1)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    eng = _engine(static, layers, 3)
+    st = FusedStep(eng, spec, adam(1e-3), resample=(4096, [0., 0.], [1., 1.], 5), use_graph=False)
+    for _ in range(2):
+        st.step()
+        torch.cuda.synchronize()
+        x = st.ps.x.cpu().numpy()
+        assert x.min() >= 0.0 and x.max() < 1.0
+        ref = _oracle_takes_for(static, x)
+        t = st.ps.takes
+        s = int(t.pt_off[t.n].item())
+        np.testing.assert_array_equal(t.n_take[:s].cpu().numpy(), ref[1])
+        np.testing.assert_array_equal(t.m_take[:s].cpu().numpy(), ref[0])
+    st.check()
+
+
+def _oracle_takes_for(static, x):
+    p = static["subdomain"]["params"]
+    takes, _, _ = OT.get_inputs(x, np.ones(static["m"], dtype=int), p[0].numpy(), p[1].numpy(),
+                                static["subdomain"]["pou"].numpy())
+    return takes
+
+
+def test_trainer_short_run_matches_oracle_training(cuda):
+    """FBPINNTrainer (fused HO hard-BC, 15 subdomains, 1-32-32-1, 200 grid points)
+    vs the oracle's Adam loop from the same initial parameters: parameters after
+    5 steps agree, and the test L1 decreases over 300 steps."""
+    from fbpinns_gb300.constants import Constants, get_subdomain_ws
+    from fbpinns_gb300.trainers import FBPINNTrainer, init_subdomain_networks
+    from fbpinns_gb300 import networks
+    sx = [np.linspace(0, 1, 15)]
+    c = Constants(problem=PR.HarmonicOscillator1DHardBC, problem_init_kwargs=dict(d=2, w0=80, sd=0.1),
+                  decomposition_init_kwargs=dict(subdomain_xs=sx, subdomain_ws=get_subdomain_ws(sx, 2.0),
+                                                 unnorm=(0., 1.)),
+                  network_init_kwargs=dict(layer_sizes=[1, 32, 32, 1]), ns=((200,),), n_test=(1000,),
+                  n_steps=5, summary_freq=5, test_freq=5, use_graph=False)
+    tr = FBPINNTrainer(c)
+    ap = tr.train()
+    got = networks.pack_layers(ap["trainable"]["network"]["subdomain"]["layers"]).double()
+    # oracle
+    static = tr.all_params["static"]["decomposition"]
+    m = static["m"]
+    _, net = init_subdomain_networks(networks.FCN, c.network_init_kwargs, m, c.seed)
+    layers = [(w.double(), b.double()) for w, b in net["layers"]]
+    P = oracle_params(static, layers, {"sd": 0.1, "mu": 4, "k": 6400})
+    x = np.linspace(0, 1, 200, dtype=np.float64).astype(np.float32).reshape(-1, 1)
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(m, dtype=int), p[0].numpy(), p[1].numpy(),
+                                                          static["subdomain"]["pou"].numpy())
+    jm = OM.get_jmaps(((0, ()), (0, (0,)), (0, (0, 0))))
+    mu = [torch.zeros_like(t) for wb in layers for t in wb]
+    nu = [torch.zeros_like(t) for wb in layers for t in wb]
+    ai = torch.as_tensor(a_ims)
+    for it in range(5):
+        _, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes], [jm],
+                                        OP.HarmonicOscillator1DHardBC)
+        flat = [t for gw in grads for t in gw]
+        new = []
+        for li, (w, b) in enumerate(P["layers"]):
+            pair = []
+            for k, t in enumerate((w, b)):
+                idx = 2 * li + k
+                g = torch.zeros_like(t)
+                g[ai] = flat[idx]
+                th, mu[idx], nu[idx], _ = OM.adam_update(t, g, mu[idx], nu[idx], it, 1e-3)
+                pair.append(th)
+            new.append(tuple(pair))
+        P["layers"] = new
+    ref = networks.pack_layers([(w, b) for w, b in P["layers"]])
+    # Adam normalises the update, so compare the parameter change after 5 steps
+    init = networks.pack_layers(layers)
+    d_got, d_ref = (got - init).numpy(), (ref - init).numpy()
+    assert rel_err(d_got, d_ref) < 1e-3
+    # and a longer run reduces the test error
+    c2 = Constants(**{k: v for k, v in vars(c).items() if k in ("problem", "problem_init_kwargs",
+                                                                 "decomposition_init_kwargs", "network_init_kwargs",
+                                                                 "ns", "n_test")},
+                   n_steps=300, summary_freq=100, test_freq=300, use_graph=True)
+    tr2 = FBPINNTrainer(c2)
+    tr2.train()
+    l1 = [r[1] for r in tr2.u_test_losses]
+    assert l1[-1] < l1[0]
