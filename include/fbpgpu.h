@@ -143,6 +143,20 @@ size_t fbp_scan_scratch_bytes(int64_t n);
 int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n,
                  void* scratch, size_t scratch_bytes, void* stream);
 
+/* Largest n accepted by fbp_scan_i32_noalloc. */
+#define FBP_SCAN_NOALLOC_MAX_N (1 << 24)
+
+/* fbp_scan_i32 without a scratch argument, for callers that cannot allocate
+ * device memory (so cannot pass a scratch buffer): its scratch is a fixed
+ * 32 KiB array inside the library, which every GPU that loads the library
+ * keeps until the process exits.  n must not exceed FBP_SCAN_NOALLOC_MAX_N
+ * (FBP_ERR_CAPACITY otherwise).  The first call on each device looks up that
+ * array's device address, so make it before capturing a stream into a CUDA
+ * graph.  All calls share the one array: calls that overlap on the GPU (for
+ * example on two streams at once) race and must be serialised by the caller.
+ * No counterpart in the reference: it is an addition of this library. */
+int fbp_scan_i32_noalloc(const int32_t* in, int32_t* out, int64_t n, void* stream);
+
 /* Count pass of the point-in-box test.  For every point: the number of
  * selected boxes that contain it (pt_count), the bit mask of their POU levels
  * (pt_lvl) and its popcount (pt_nlvl).  model_count (nullable) receives the
