@@ -21,7 +21,6 @@ static int dispatch(int mode, const fbp_net* net, const float* x, const fbp_pair
     int rc = check_net(net, pr);
     if (rc) return rc;
     FBP_REQUIRE(x && out, FBP_ERR_INVALID, "jet: null x/out");
-    if (grid <= 0) grid = sm_count() * 4;
     cudaStream_t st = as_stream(stream);
     int r = jet_group_a(mode, net, x, pr, slot_out, out, grid, st);
     if (r != 1) return r;

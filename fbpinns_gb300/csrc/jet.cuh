@@ -106,7 +106,7 @@ __device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, floa
 template <class C>
 __device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J], float& a, float& tp,
                                          float& tpp) {
-    a = tanhf(z[0]);
+    a = tanh_fast(z[0]);
     tp = 1.0f - a * a;
     tpp = -2.0f * a * tp;
     g[0] = a;
@@ -193,7 +193,7 @@ __device__ __forceinline__ float l1_act(const SParams<C>& S, const float (&xn)[C
     float z = S.b1[n];
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) z = fmaf(S.W1[n * C::XD + d], xn[d], z);
-    return tanhf(z);
+    return tanh_fast(z);
 }
 
 // Layer-2 z-jets for neurons [k0, k0+KC) from first-layer activations a1row[n*stride]

@@ -6,11 +6,25 @@
 
 namespace fbp {
 
+// Persistent grid: every CTA that can be resident at once (occupancy x SMs).
+template <class K>
+int resident_grid(K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * sm_count();
+}
+
 template <int XD, int H1, int H2, int D2>
 int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, float* pair_out, int grid,
                    cudaStream_t st) {
     using C = Cfg<XD, H1, H2, D2>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward: nparam %d != %d for this shape", net.nparam, C::P);
+    static int auto_grid = 0;
+    if (grid <= 0) {
+        if (!auto_grid) auto_grid = resident_grid(forward_pairs_kernel<C>, FWD_THREADS, 0);
+        grid = auto_grid;
+    }
     forward_pairs_kernel<C><<<grid, FWD_THREADS, 0, st>>>(net, x, pr, pair_out);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
@@ -23,9 +37,14 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "adjoint: nparam %d != %d for this shape", net.nparam, C::P);
     const size_t shm = sizeof(SAdj<C>);
     static bool attr_set = false;
+    static int auto_grid = 0;
     if (!attr_set) {
         FBP_CUDA_CHECK(cudaFuncSetAttribute(adjoint_pairs_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
         attr_set = true;
+    }
+    if (grid <= 0) {
+        if (!auto_grid) auto_grid = resident_grid(adjoint_pairs_kernel<C>, AdjT<C>::T, shm);
+        grid = auto_grid;
     }
     adjoint_pairs_kernel<C><<<grid, AdjT<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
     FBP_LAUNCH_CHECK();

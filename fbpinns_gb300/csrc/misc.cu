@@ -123,6 +123,11 @@ __global__ void fma_probe_kernel(float* sink, int iters) {
     if (s == 12345.678f) sink[threadIdx.x] = s;  // keeps the chains live
 }
 
+__global__ void tanh_probe_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = tanh_fast(x[i]);
+}
+
 }  // namespace fbp
 
 using namespace fbp;
@@ -173,5 +178,14 @@ extern "C" int fbp_fma_probe(float* sink, int32_t blocks, int32_t iters, double*
     fma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(sink, iters);
     FBP_LAUNCH_CHECK();
     *flops_out = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;
+    return FBP_OK;
+}
+
+extern "C" int fbp_tanh_probe(const float* x, float* y, int64_t n, void* stream) {
+    FBP_REQUIRE(x && y && n >= 0, FBP_ERR_INVALID, "fbp_tanh_probe: bad args");
+    if (n == 0) return FBP_OK;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+    tanh_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(x, y, n);
+    FBP_LAUNCH_CHECK();
     return FBP_OK;
 }

@@ -132,7 +132,7 @@ class PointSet:
         eng = self.eng
         lib = _lib.load()
         st = _lib.stream_ptr(stream)
-        sizes = self.takes.build(self.x, self.select, stream)
+        sizes = self.takes.build(self.x, self.select, stream, count_models=False)
         if sizes is not None:
             s, u = sizes
             if not self._sized or s > self.s_cap or u > self.u_cap:
@@ -174,6 +174,11 @@ class PointSet:
         p.items_cap = self.items_cap
         p.slots_cap = self.slot_out.shape[0]
         return p
+
+    def subdomain_counts(self):
+        """Pairs per subdomain (from the subdomain-major order), int64 on the device."""
+        st = self.sd_start.long()
+        return st[1:] - st[:-1]
 
     def check_status(self):
         self.takes.check_status()

@@ -102,20 +102,26 @@ class PointTakes:
         if getattr(self, "np_take", None) is None or self.np_take.numel() < u_cap:
             self.np_take = torch.empty(max(u_cap, 1), dtype=torch.int32, device=dev)
 
-    def build(self, x, select=None, stream=None):
+    def build(self, x, select=None, stream=None, count_models=True):
         """Count, scan and fill for points x (n, xd) float32 on the device.
 
-        Returns (s, u) as python ints when sizes were read back, else None.
+        ``count_models`` also fills ``model_count`` (points per box, with
+        atomics); the training step leaves it off and reads the per-subdomain
+        counts from the pair sort instead.  Returns (s, u) as python ints when
+        sizes were read back, else None.
         """
         lib = _lib.load()
         st = _lib.stream_ptr(stream)
         b = self.grid.boxes(select)
         assert x.is_cuda and x.dtype == torch.float32 and x.shape == (self.n, self.grid.xd)
         x = x.contiguous()
-        self.model_count.zero_()  # the status word is sticky: cleared only by reset_status()
+        # the status word is sticky: cleared only by reset_status()
+        if count_models:
+            self.model_count.zero_()
         _lib.check(lib.fbp_inside_count(_lib.ptr(x), self.n, C.byref(b), _lib.ptr(self.pt_count),
-                                        _lib.ptr(self.pt_nlvl), _lib.ptr(self.pt_lvl), _lib.ptr(self.model_count),
-                                        st), "fbp_inside_count")
+                                        _lib.ptr(self.pt_nlvl), _lib.ptr(self.pt_lvl),
+                                        _lib.ptr(self.model_count) if count_models else None, st),
+                   "fbp_inside_count")
         sb = self._scan_scratch.numel() * 4
         _lib.check(lib.fbp_scan_i32(_lib.ptr(self.pt_count), _lib.ptr(self.pt_off), self.n,
                                     _lib.ptr(self._scan_scratch), sb, st), "fbp_scan_i32")

@@ -302,7 +302,7 @@ class FBPINNTrainer:
                 state[state == 0] = 1
                 if xs_for_mask is not None and xs_for_mask.shape[0]:
                     tk = eng.points(xs_for_mask.to(dev))
-                    has = (tk.takes.model_count > 0).cpu().numpy()
+                    has = (tk.subdomain_counts() > 0).cpu().numpy()
                     del tk
                 else:
                     has = np.ones(m, dtype=bool)

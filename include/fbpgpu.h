@@ -289,6 +289,11 @@ int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, cons
  * flop count of the launch. */
 int fbp_fma_probe(float* sink, int32_t blocks, int32_t iters, double* flops_out, void* stream);
 
+/* Evaluates the device tanh used inside the jet kernels, y[i] = tanh(x[i]),
+ * so that its error can be checked against a reference tanh.  No counterpart
+ * in the reference (which calls jnp.tanh, fbpinns/networks.py:64). */
+int fbp_tanh_probe(const float* x, float* y, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -360,3 +360,18 @@ def test_trainer_short_run_matches_oracle_training(cuda):
     tr2.train()
     l1 = [r[1] for r in tr2.u_test_losses]
     assert l1[-1] < l1[0]
+
+
+def test_fast_tanh_error(cuda):
+    """The device tanh of the jet kernels vs torch's float64 tanh: absolute error
+    below 2.5e-7 over [-20, 20] (the jets need absolute accuracy)."""
+    from fbpinns_gb300 import _lib
+    lib = _lib.load()
+    x = torch.cat([torch.linspace(-20, 20, 2_000_001), torch.linspace(-1e-3, 1e-3, 100_001),
+                   torch.tensor([0.0, -0.0, 1e-30, -1e-30, 80.0, -80.0])]).to(cuda)
+    y = torch.empty_like(x)
+    _lib.check(lib.fbp_tanh_probe(_lib.ptr(x), _lib.ptr(y), x.numel(), _lib.stream_ptr()), "fbp_tanh_probe")
+    ref = torch.tanh(x.double())
+    err = (y.double() - ref).abs().max().item()
+    assert err < 2.5e-7, err
+    assert torch.all(y.abs() <= 1.0)
