@@ -304,37 +304,43 @@ __global__ void __launch_bounds__(FWD_THREADS) forward_pairs_kernel(fbp_net net,
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint.  Per tile of T pairs (one per thread):
-//  A (thread = pair): seed -> o-bar through the window product and
+// Adjoint.  Each warp of a CTA walks 32-pair tiles of the CTA's work item on
+// its own (only __syncwarp inside an item; the CTA syncs only to load the
+// subdomain's weights and to combine the warps' gradient sums at the end):
+//  A (lane = pair): seed -> o-bar through the window product and the
 //    unnormalisation; recompute layer 1 and, chunk by chunk, layer 2; tanh-jet
-//    adjoint -> z2-bar, staged in shared memory with a1 and the small terms.
-//  B (thread = pair): v-bar = W2^T z2-bar from its own staged row; layer-1
-//    jet adjoint -> z1-bar and the d(cw)-bar terms, staged.
-//  C (thread = gradient entry): deterministic sums over the tile's pairs,
-//    accumulated per work item in shared memory; written once per item.
+//    adjoint -> z2-bar, staged in the warp's shared rows with a1.
+//  B (lane = pair): v-bar = W2^T z2-bar from its own row; layer-1 jet adjoint.
+//  C (lane = 4x2 block of W2-bar): sum over the tile's pairs from the rows.
+// The per-lane gradient terms of W3, W1 and the biases are summed over the
+// 32 lanes by a deterministic reduce-scatter butterfly (no shared staging);
+// every sum has a fixed order, so results are bitwise reproducible.
 // ---------------------------------------------------------------------------
+__host__ __device__ constexpr int pow2_at_least(int v) {
+    int p = 32;
+    while (p < v) p <<= 1;
+    return p;
+}
+
 template <class C>
-struct AdjT {
-    static constexpr int T = (C::H1 >= 32 || C::H2 >= 32) ? 64 : 128;  // pairs per tile = threads
-    static constexpr int ZS = ((C::HL * C::J + 7) / 8) * 8 + 4;       // z2-bar row stride (floats)
-    static constexpr int AS = C::H1 + 1;                              // a1 row stride
-    static constexpr int KB = 4;                                      // W2-bar rows per thread block
-    static constexpr int NBLK = C::TWO ? (C::H2 / KB) * C::H1 : 1;    // (k-block, n) outputs
-    static constexpr int G = C::TWO ? (T >= NBLK ? T / NBLK : 1) : 1; // t-split groups
-    static_assert(!C::TWO || C::H2 % KB == 0, "H2 multiple of 4");
+struct AdjW {
+    static constexpr int ZS = ((C::HL * C::J + 7) / 8) * 8 + 4;   // z2-bar row stride (floats): 16-B rows,
+                                                                  // conflict-free 128-bit access per 8-lane phase
+    static constexpr int AS = C::H1 + 1;                          // a1 row stride
+    static constexpr int W = ZS <= 96 ? 4 : 2;                    // warps per CTA
+    static constexpr int T = 32 * W;
+    static constexpr int KB = 4, NB = 2;                          // W2-bar block per lane
+    static constexpr int NBLK = C::TWO ? (C::H2 / KB) * (C::H1 / NB) : 0;
+    static constexpr int PASSES = C::TWO ? (NBLK + 31) / 32 : 0;
+    static_assert(!C::TWO || (C::H2 % KB == 0 && C::H1 % NB == 0), "W2 blocking");
 };
 
 template <class C>
-struct SAdj {
-    float zb[C::TWO ? AdjT<C>::T * AdjT<C>::ZS : 4];  // [t][c][k] z2-bar jets
-    float a1[AdjT<C>::T * AdjT<C>::AS];               // [t][n]
-    float e3[AdjT<C>::T * (C::HL + 1)];               // [t][k] sum_c obar_c g_c[k]
-    float g1[AdjT<C>::T * AdjT<C>::AS];               // [t][n] z1-bar
-    float gc[AdjT<C>::T * C::H1 * C::XD + 4];         // [t][n][d] cw-bar
-    float xn[AdjT<C>::T * C::XD];
-    float ob0[AdjT<C>::T];
-    // per-item gradient accumulators
-    float gW2[C::TWO ? AdjT<C>::G * C::H2 * C::H1 : 4];
+struct WarpRows {
+    float zb[C::TWO ? 32 * AdjW<C>::ZS : 4];  // [t][c][k]
+    float a1[32 * AdjW<C>::AS];                 // [t][n]
+    // warp gradient sums over its tiles of the item
+    float gW2[C::TWO ? C::H2 * C::H1 : 4];
     float gW1[C::H1 * C::XD];
     float gb1[C::H1];
     float gb2[C::TWO ? C::H2 : 4];
@@ -342,39 +348,62 @@ struct SAdj {
     float gb3;
 };
 
+// Reduce-scatter over the warp: v[NV] per lane -> lane L holds the warp sums of
+// indices [L*NV/32, (L+1)*NV/32) in v[0 .. NV/32).
+template <int NV>
+__device__ __forceinline__ void warp_reduce_scatter(float (&v)[NV], int lane) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+        const int m = 16 >> r;
+        const int half = NV >> (r + 1);
+        const bool upper = (lane & m) != 0;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const float keep = upper ? v[i + half] : v[i];
+            const float send = upper ? v[i] : v[i + half];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+        }
+    }
+}
+
 template <class C>
-__global__ void __launch_bounds__(AdjT<C>::T) adjoint_pairs_kernel(fbp_net net, const float* __restrict__ x,
+__global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, const float* __restrict__ x,
                                                                    fbp_pairs pr, const float* __restrict__ slot_out,
                                                                    float* __restrict__ grad_part) {
-    using A = AdjT<C>;
-    constexpr int T = A::T, J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2, HL = C::HL;
+    using A = AdjW<C>;
+    constexpr int J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2, HL = C::HL, NW = A::W;
     __shared__ SParams<C> S;
     extern __shared__ float4 dyn_smem[];
-    SAdj<C>& R = *reinterpret_cast<SAdj<C>*>(dyn_smem);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    WarpRows<C>& R = reinterpret_cast<WarpRows<C>*>(dyn_smem)[wid];
     const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
     for (int it = blockIdx.x; it < nit; it += gridDim.x) {
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
         load_params<C>(S, net, j);
-        // zero the item accumulators
         if constexpr (C::TWO)
-            for (int i = tid; i < A::G * H2 * H1; i += T) R.gW2[i] = 0.f;
-        for (int i = tid; i < H1 * XD; i += T) R.gW1[i] = 0.f;
-        for (int i = tid; i < H1; i += T) R.gb1[i] = 0.f;
+            for (int i = lane; i < H2 * H1; i += 32) R.gW2[i] = 0.f;
+        for (int i = lane; i < H1 * XD; i += 32) R.gW1[i] = 0.f;
+        for (int i = lane; i < H1; i += 32) R.gb1[i] = 0.f;
         if constexpr (C::TWO)
-            for (int i = tid; i < H2; i += T) R.gb2[i] = 0.f;
-        for (int i = tid; i < HL; i += T) R.gW3[i] = 0.f;
-        if (tid == 0) R.gb3 = 0.f;
-        __syncthreads();
-        for (int t0 = 0; t0 < cnt; t0 += T) {
-            const int nt = min(T, cnt - t0);
+            for (int i = lane; i < H2; i += 32) R.gb2[i] = 0.f;
+        for (int i = lane; i < HL; i += 32) R.gW3[i] = 0.f;
+        if (lane == 0) R.gb3 = 0.f;
+        __syncwarp();
+        for (int t0 = wid * 32; t0 < cnt; t0 += A::T) {
+            const int nt = min(32, cnt - t0);
+            const bool act = lane < nt;
             // ---------------- phase A ----------------
-            if (tid < nt) {
-                const int e = beg + t0 + tid;
+            float ob[J], xn[XD];  // the lane's o-bar jet and normalised point, kept for phase B
+#pragma unroll
+            for (int c = 0; c < J; ++c) ob[c] = 0.f;
+#pragma unroll
+            for (int d = 0; d < XD; ++d) xn[d] = 0.f;
+            float* a1row = &R.a1[lane * A::AS];
+            if (act) {
+                const int e = beg + t0 + lane;
                 const int pt = pr.sd_point[e];
                 const int slot = pr.sd_slot[e];
-                float xn[XD];
                 load_point<C>(S, x, pt, xn);
                 float w[J];
                 window_jet<C>(S, xn, w);
@@ -398,18 +427,22 @@ __global__ void __launch_bounds__(AdjT<C>::T) adjoint_pairs_kernel(fbp_net net, 
                     ub[1 + d] += 2.0f * g * w[1 + d];
                     ub[1 + XD + s] = g * w[0];
                 }
-                float ob[J];
 #pragma unroll
                 for (int c = 0; c < J; ++c) ob[c] = ub[c] * S.sd_u;
-                R.ob0[tid] = ob[0];
-#pragma unroll
-                for (int d = 0; d < XD; ++d) R.xn[tid * XD + d] = xn[d];
-                float* a1row = &R.a1[tid * A::AS];
 #pragma unroll 4
                 for (int n = 0; n < H1; ++n) a1row[n] = l1_act<C>(S, xn, n);
-                if constexpr (C::TWO) {
+            }
+            // W3-bar terms sum_c o-bar_c g_c[k], chunk by chunk of <= 32 neurons, summed over
+            // the warp by a reduce-scatter (lane k of the chunk receives neuron k's sum)
+            constexpr int KCH = C::TWO ? C::KC : HL;
 #pragma unroll 1
-                    for (int ch = 0; ch < C::NCH; ++ch) {
+            for (int ch = 0; ch < (C::TWO ? C::NCH : 1); ++ch) {
+                float e3[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) e3[k] = 0.f;
+                if (act) {
+                    if constexpr (C::TWO) {
+                        float* zrow = &R.zb[lane * A::ZS];
                         float acc[C::KC][J];
                         l2_chunk<C>(S, a1row, 1, ch * C::KC, acc);
 #pragma unroll
@@ -417,67 +450,65 @@ __global__ void __launch_bounds__(AdjT<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             const int kk = ch * C::KC + k;
                             float g[J], a, tp, tpp;
                             tanh_jet<C>(acc[k], g, a, tp, tpp);
-                            float e3 = 0.f;
                             float gb[J];
                             const float w3 = S.W3[kk];
+                            float s3 = 0.f;
 #pragma unroll
                             for (int c = 0; c < J; ++c) {
-                                e3 = fmaf(ob[c], g[c], e3);
+                                s3 = fmaf(ob[c], g[c], s3);
                                 gb[c] = w3 * ob[c];
                             }
-                            R.e3[tid * (HL + 1) + kk] = e3;
+                            e3[k] = s3;
                             float zb[J];
                             tanh_jet_adj<C>(acc[k], a, tp, tpp, gb, zb);
 #pragma unroll
-                            for (int c = 0; c < J; ++c) R.zb[tid * A::ZS + c * H2 + kk] = zb[c];
-                        }
-                    }
-                } else {
-                    // single hidden layer: output layer reads the layer-1 jets directly
-#pragma unroll 2
-                    for (int n = 0; n < H1; ++n) {
-                        float v[J];
-                        l1_jet<C>(S, n, a1row[n], v);
-                        float e3 = 0.f;
-#pragma unroll
-                        for (int c = 0; c < J; ++c) e3 = fmaf(ob[c], v[c], e3);
-                        R.e3[tid * (HL + 1) + n] = e3;
-                        // v-bar = W3[n] * ob  -> layer-1 jet adjoint
-                        const float w3 = S.W3[n];
-                        const float a = a1row[n], tp = 1.0f - a * a, tpp = -2.0f * a * tp;
-                        float tpb = 0.f, tppb = 0.f;
-#pragma unroll
-                        for (int d = 0; d < XD; ++d) {
-                            const float vb = w3 * ob[1 + d];
-                            tpb += vb * S.cw[n * XD + d];
-                            R.gc[(tid * H1 + n) * XD + d] = vb * tp;
+                            for (int c = 0; c < J; ++c) acc[k][c] = zb[c];
                         }
 #pragma unroll
-                        for (int s = 0; s < C::NS; ++s) {
-                            const int d = C::sd_dim(s);
-                            const float vb = w3 * ob[1 + XD + s];
-                            const float cwd = S.cw[n * XD + d];
-                            tppb += vb * cwd * cwd;
-                            R.gc[(tid * H1 + n) * XD + d] += 2.0f * vb * tpp * cwd;
+                        for (int c = 0; c < J; ++c)
+#pragma unroll
+                            for (int q = 0; q < C::KC; q += 4)
+                                *reinterpret_cast<float4*>(zrow + c * H2 + ch * C::KC + q) =
+                                    make_float4(acc[q][c], acc[q + 1][c], acc[q + 2][c], acc[q + 3][c]);
+                    } else {
+#pragma unroll
+                        for (int n = 0; n < H1; ++n) {
+                            float v[J];
+                            l1_jet<C>(S, n, a1row[n], v);
+                            float s3 = 0.f;
+#pragma unroll
+                            for (int c = 0; c < J; ++c) s3 = fmaf(ob[c], v[c], s3);
+                            e3[n] = s3;
                         }
-                        const float ab = w3 * ob[0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f);
-                        R.g1[tid * A::AS + n] = ab * tp;
                     }
                 }
+                warp_reduce_scatter<32>(e3, lane);
+                if (lane < KCH) R.gW3[ch * KCH + lane] += e3[0];
             }
-            __syncthreads();
-            // ---------------- phase B (two hidden layers) ----------------
-            if constexpr (C::TWO) {
-                if (tid < nt) {
-                    const float* zrow = &R.zb[tid * A::ZS];
-                    constexpr int NC = 8 < H1 ? 8 : H1;
+            const float ob0 = ob[0];
+            float b3 = ob0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) b3 += __shfl_xor_sync(0xffffffffu, b3, o);
+            if (lane == 0) R.gb3 += b3;
+            __syncwarp();
+            // ---------------- phase B: layer-1 adjoint ----------------
+            // per chunk of NC first-layer neurons: v-bar = W2^T z2-bar (own row), the
+            // layer-1 jet adjoint, and the W1-bar / b1-bar terms summed over the warp
+            constexpr int NC = 8 < H1 ? 8 : H1;
+            static_assert(NC * (XD + 1) <= 32, "layer-1 chunk must fit one reduce-scatter");
 #pragma unroll 1
-                    for (int n0 = 0; n0 < H1; n0 += NC) {
-                        float vb[NC][J];
+            for (int n0 = 0; n0 < H1; n0 += NC) {
+                float r1[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) r1[i] = 0.f;
+                if (act) {
+                    float vb[NC][J];
+                    if constexpr (C::TWO) {
 #pragma unroll
                         for (int q = 0; q < NC; ++q)
 #pragma unroll
                             for (int c = 0; c < J; ++c) vb[q][c] = 0.f;
+                        const float* zrow = &R.zb[lane * A::ZS];
 #pragma unroll 1
                         for (int k0 = 0; k0 < H2; k0 += 4) {
                             float4 z4[J];
@@ -497,119 +528,160 @@ __global__ void __launch_bounds__(AdjT<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                 }
                             }
                         }
+                    } else {
 #pragma unroll
                         for (int q = 0; q < NC; ++q) {
-                            const int n = n0 + q;
-                            const float a = R.a1[tid * A::AS + n];
-                            const float tp = 1.0f - a * a, tpp = -2.0f * a * tp;
-                            float tpb = 0.f, tppb = 0.f;
+                            const float w3 = S.W3[n0 + q];
 #pragma unroll
-                            for (int d = 0; d < XD; ++d) {
-                                tpb += vb[q][1 + d] * S.cw[n * XD + d];
-                                R.gc[(tid * H1 + n) * XD + d] = vb[q][1 + d] * tp;
-                            }
-#pragma unroll
-                            for (int s = 0; s < C::NS; ++s) {
-                                const int d = C::sd_dim(s);
-                                const float g = vb[q][1 + XD + s];
-                                const float cwd = S.cw[n * XD + d];
-                                tppb += g * cwd * cwd;
-                                R.gc[(tid * H1 + n) * XD + d] += 2.0f * g * tpp * cwd;
-                            }
-                            const float ab = vb[q][0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f);
-                            R.g1[tid * A::AS + n] = ab * tp;
+                            for (int c = 0; c < J; ++c) vb[q][c] = w3 * ob[c];
                         }
                     }
-                }
-                __syncthreads();
-            }
-            // ---------------- phase C: tile reductions ----------------
-            if constexpr (C::TWO) {
-                // W2-bar[k][n] = sum_t sum_c zb[t][c][k] v_c[t][n],
-                // v_0 = a, v_d = t' cw[n][d], v_dd = t'' cw[n][d]^2
-                for (int b = tid; b < A::NBLK * A::G; b += T) {
-                    const int blk = b % A::NBLK, g = b / A::NBLK;
-                    const int n = blk % H1, k0 = (blk / H1) * A::KB;
-                    float s[A::KB][J];
 #pragma unroll
-                    for (int q = 0; q < A::KB; ++q)
-#pragma unroll
-                        for (int c = 0; c < J; ++c) s[q][c] = 0.f;
-                    for (int t = g; t < nt; t += A::G) {
-                        const float a = R.a1[t * A::AS + n];
+                    for (int q = 0; q < NC; ++q) {
+                        const int n = n0 + q;
+                        const float a = a1row[n];
                         const float tp = 1.0f - a * a, tpp = -2.0f * a * tp;
-                        const float* zr = &R.zb[t * A::ZS + k0];
+                        float tpb = 0.f, tppb = 0.f, cwb[XD];
 #pragma unroll
-                        for (int c = 0; c < J; ++c) {
-                            const float4 z4 = *reinterpret_cast<const float4*>(zr + c * H2);
-                            const float m = (c == 0) ? a : (c <= XD ? tp : tpp);
-                            s[0][c] = fmaf(z4.x, m, s[0][c]);
-                            s[1][c] = fmaf(z4.y, m, s[1][c]);
-                            s[2][c] = fmaf(z4.z, m, s[2][c]);
-                            s[3][c] = fmaf(z4.w, m, s[3][c]);
+                        for (int d = 0; d < XD; ++d) {
+                            tpb += vb[q][1 + d] * S.cw[n * XD + d];
+                            cwb[d] = vb[q][1 + d] * tp;
+                        }
+#pragma unroll
+                        for (int s = 0; s < C::NS; ++s) {
+                            const int d = C::sd_dim(s);
+                            const float g = vb[q][1 + XD + s];
+                            const float cwd = S.cw[n * XD + d];
+                            tppb += g * cwd * cwd;
+                            cwb[d] += 2.0f * g * tpp * cwd;
+                        }
+                        const float z1b = (vb[q][0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f)) * tp;
+#pragma unroll
+                        for (int d = 0; d < XD; ++d) r1[q * (XD + 1) + d] = fmaf(z1b, xn[d], cwb[d] * S.inv_sd[d]);
+                        r1[q * (XD + 1) + XD] = z1b;
+                    }
+                }
+                warp_reduce_scatter<32>(r1, lane);
+                if (lane < NC * (XD + 1)) {
+                    const int q = lane / (XD + 1), d = lane - q * (XD + 1);
+                    if (d < XD)
+                        R.gW1[(n0 + q) * XD + d] += r1[0];
+                    else
+                        R.gb1[n0 + q] += r1[0];
+                }
+            }
+            // ---------------- phase C: W2-bar over the tile ----------------
+            if constexpr (C::TWO) {
+#pragma unroll 1
+                for (int ps = 0; ps < A::PASSES; ++ps) {
+                    const int b = ps * 32 + lane;
+                    if (b < A::NBLK) {
+                        const int nb = b % (H1 / A::NB), kb = b / (H1 / A::NB);
+                        const int n0 = nb * A::NB, k0 = kb * A::KB;
+                        float sacc[A::KB][A::NB][J];
+#pragma unroll
+                        for (int i = 0; i < A::KB; ++i)
+#pragma unroll
+                            for (int q = 0; q < A::NB; ++q)
+#pragma unroll
+                                for (int c = 0; c < J; ++c) sacc[i][q][c] = 0.f;
+                        float b2s[A::KB] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+                        for (int t = 0; t < nt; ++t) {
+                            float m[A::NB][3];
+#pragma unroll
+                            for (int q = 0; q < A::NB; ++q) {
+                                const float a = R.a1[t * A::AS + n0 + q];
+                                const float tp = 1.0f - a * a;
+                                m[q][0] = a;
+                                m[q][1] = tp;
+                                m[q][2] = -2.0f * a * tp;
+                            }
+                            const float* zr = &R.zb[t * A::ZS + k0];
+#pragma unroll
+                            for (int c = 0; c < J; ++c) {
+                                const float4 z4 = *reinterpret_cast<const float4*>(zr + c * H2);
+                                const int mi = c == 0 ? 0 : (c <= XD ? 1 : 2);
+                                if (c == 0) {
+                                    b2s[0] += z4.x;
+                                    b2s[1] += z4.y;
+                                    b2s[2] += z4.z;
+                                    b2s[3] += z4.w;
+                                }
+#pragma unroll
+                                for (int q = 0; q < A::NB; ++q) {
+                                    const float mm = m[q][mi];
+                                    sacc[0][q][c] = fmaf(z4.x, mm, sacc[0][q][c]);
+                                    sacc[1][q][c] = fmaf(z4.y, mm, sacc[1][q][c]);
+                                    sacc[2][q][c] = fmaf(z4.z, mm, sacc[2][q][c]);
+                                    sacc[3][q][c] = fmaf(z4.w, mm, sacc[3][q][c]);
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int i = 0; i < A::KB; ++i)
+#pragma unroll
+                            for (int q = 0; q < A::NB; ++q) {
+                                const int n = n0 + q;
+                                float v = sacc[i][q][0];
+#pragma unroll
+                                for (int d = 0; d < XD; ++d) v = fmaf(S.cw[n * XD + d], sacc[i][q][1 + d], v);
+#pragma unroll
+                                for (int ss = 0; ss < C::NS; ++ss)
+                                    v = fmaf(S.cw2[n * XD + C::sd_dim(ss)], sacc[i][q][1 + XD + ss], v);
+                                R.gW2[(k0 + i) * H1 + n] += v;
+                            }
+                        if (nb == 0) {
+#pragma unroll
+                            for (int i = 0; i < A::KB; ++i) R.gb2[k0 + i] += b2s[i];
                         }
                     }
-#pragma unroll
-                    for (int q = 0; q < A::KB; ++q) {
-                        float v = s[q][0];
-#pragma unroll
-                        for (int d = 0; d < XD; ++d) v = fmaf(S.cw[n * XD + d], s[q][1 + d], v);
-#pragma unroll
-                        for (int ss = 0; ss < C::NS; ++ss) v = fmaf(S.cw2[n * XD + C::sd_dim(ss)], s[q][1 + XD + ss], v);
-                        R.gW2[(g * H2 + k0 + q) * H1 + n] += v;
-                    }
-                }
-                // b2-bar[k] = sum_t zb[t][0][k]
-                for (int k = tid; k < H2; k += T) {
-                    float acc = 0.f;
-                    for (int t = 0; t < nt; ++t) acc += R.zb[t * A::ZS + k];
-                    R.gb2[k] += acc;
                 }
             }
-            for (int k = tid; k < HL; k += T) {
-                float acc = 0.f;
-                for (int t = 0; t < nt; ++t) acc += R.e3[t * (HL + 1) + k];
-                R.gW3[k] += acc;
-            }
-            if (tid == 0) {
-                float acc = 0.f;
-                for (int t = 0; t < nt; ++t) acc += R.ob0[t];
-                R.gb3 += acc;
-            }
-            for (int n = tid; n < H1; n += T) {
-                float sb = 0.f, sw[XD], sc[XD];
-#pragma unroll
-                for (int d = 0; d < XD; ++d) sw[d] = sc[d] = 0.f;
-                for (int t = 0; t < nt; ++t) {
-                    const float g = R.g1[t * A::AS + n];
-                    sb += g;
-#pragma unroll
-                    for (int d = 0; d < XD; ++d) {
-                        sw[d] = fmaf(g, R.xn[t * XD + d], sw[d]);
-                        sc[d] += R.gc[(t * H1 + n) * XD + d];
-                    }
-                }
-                R.gb1[n] += sb;
-#pragma unroll
-                for (int d = 0; d < XD; ++d) R.gW1[n * XD + d] += sw[d] + sc[d] * S.inv_sd[d];
-            }
-            __syncthreads();
+            __syncwarp();
         }
-        // write the item's gradient partial in the packed theta layout
+        __syncthreads();
+        // combine the warps' sums (fixed warp order) into the item's gradient partial
         float* dst = grad_part + (size_t)it * C::P;
-        for (int i = tid; i < H1 * XD; i += T) dst[C::oW1 + i] = R.gW1[i];
-        for (int i = tid; i < H1; i += T) dst[C::ob1 + i] = R.gb1[i];
+        WarpRows<C>* RW = reinterpret_cast<WarpRows<C>*>(dyn_smem);
+        for (int i = tid; i < H1 * XD; i += blockDim.x) {
+            float v = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) v += RW[w].gW1[i];
+            dst[C::oW1 + i] = v;
+        }
+        for (int i = tid; i < H1; i += blockDim.x) {
+            float v = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) v += RW[w].gb1[i];
+            dst[C::ob1 + i] = v;
+        }
         if constexpr (C::TWO) {
-            for (int i = tid; i < H2 * H1; i += T) {
+            for (int i = tid; i < H2 * H1; i += blockDim.x) {
                 float v = 0.f;
 #pragma unroll
-                for (int g = 0; g < A::G; ++g) v += R.gW2[g * H2 * H1 + i];
+                for (int w = 0; w < NW; ++w) v += RW[w].gW2[i];
                 dst[C::oW2 + i] = v;
             }
-            for (int i = tid; i < H2; i += T) dst[C::ob2 + i] = R.gb2[i];
+            for (int i = tid; i < H2; i += blockDim.x) {
+                float v = 0.f;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) v += RW[w].gb2[i];
+                dst[C::ob2 + i] = v;
+            }
         }
-        for (int i = tid; i < HL; i += T) dst[C::oW3 + i] = R.gW3[i];
-        if (tid == 0) dst[C::ob3] = R.gb3;
+        for (int i = tid; i < HL; i += blockDim.x) {
+            float v = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) v += RW[w].gW3[i];
+            dst[C::oW3 + i] = v;
+        }
+        if (tid == 0) {
+            float v = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) v += RW[w].gb3;
+            dst[C::ob3] = v;
+        }
     }
 }
 

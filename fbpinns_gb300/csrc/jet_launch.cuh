@@ -35,7 +35,7 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
                    float* grad_part, int grid, cudaStream_t st) {
     using C = Cfg<XD, H1, H2, D2>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "adjoint: nparam %d != %d for this shape", net.nparam, C::P);
-    const size_t shm = sizeof(SAdj<C>);
+    const size_t shm = sizeof(WarpRows<C>) * AdjW<C>::W;
     static bool attr_set = false;
     static int auto_grid = 0;
     if (!attr_set) {
@@ -43,10 +43,10 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
         attr_set = true;
     }
     if (grid <= 0) {
-        if (!auto_grid) auto_grid = resident_grid(adjoint_pairs_kernel<C>, AdjT<C>::T, shm);
+        if (!auto_grid) auto_grid = resident_grid(adjoint_pairs_kernel<C>, AdjW<C>::T, shm);
         grid = auto_grid;
     }
-    adjoint_pairs_kernel<C><<<grid, AdjT<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
+    adjoint_pairs_kernel<C><<<grid, AdjW<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
 }
