@@ -335,8 +335,10 @@ struct AdjW {
     static_assert(!C::TWO || (C::H2 % KB == 0 && C::H1 % NB == 0), "W2 blocking");
 };
 
+// One warp's rows; 16-byte aligned so that every warp's z2-bar rows (read and
+// written as float4) start on a 16-byte boundary in the array of WarpRows.
 template <class C>
-struct WarpRows {
+struct __align__(16) WarpRows {
     float zb[C::TWO ? 32 * AdjW<C>::ZS : 4];  // [t][c][k]
     float a1[32 * AdjW<C>::AS];                 // [t][n]
     // warp gradient sums over its tiles of the item
@@ -372,6 +374,8 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                                                    float* __restrict__ grad_part) {
     using A = AdjW<C>;
     constexpr int J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2, HL = C::HL, NW = A::W;
+    static_assert(sizeof(WarpRows<C>) % 16 == 0 && A::ZS % 4 == 0 && H2 % 4 == 0 && C::KC % 4 == 0,
+                  "float4 rows need 16-byte alignment");
     __shared__ SParams<C> S;
     extern __shared__ float4 dyn_smem[];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
