@@ -374,8 +374,8 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                                                    float* __restrict__ grad_part) {
     using A = AdjW<C>;
     constexpr int J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2, HL = C::HL, NW = A::W;
-    static_assert(sizeof(WarpRows<C>) % 16 == 0 && A::ZS % 4 == 0 && H2 % 4 == 0 && C::KC % 4 == 0,
-                  "float4 rows need 16-byte alignment");
+    static_assert(sizeof(WarpRows<C>) % 16 == 0, "warp rows must keep 16-byte alignment");
+    static_assert(!C::TWO || (A::ZS % 4 == 0 && H2 % 4 == 0 && C::KC % 4 == 0), "float4 z2-bar rows");
     __shared__ SParams<C> S;
     extern __shared__ float4 dyn_smem[];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
