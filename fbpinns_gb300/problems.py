@@ -327,7 +327,7 @@ class Poisson2D(Problem):
         for k in range(1, all_params["static"]["problem"]["n_freq"] + 1):
             a = (2 ** k) * math.pi
             u = u + torch.sin(a * x) * torch.sin(a * y) / (2 ** k)
-        return u.float()
+        return u.to(x_batch.dtype)
 
     @classmethod
     def fused_spec(cls, all_params):

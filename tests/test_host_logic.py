@@ -1,0 +1,264 @@
+"""Host-side logic (no GPU): the product's decompositions, schedulers, windows,
+networks, samplers and exact solutions against golden vectors from the
+reference's own code, the cell grid's completeness property, and the C ABI
+library's exported symbols."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from fbpinns_gb300 import decompositions as D, schedulers as S, windows as Wn, networks as N
+from fbpinns_gb300 import problems as PR, domains as DOM
+from fbpinns_gb300.constants import Constants, get_subdomain_ws
+
+
+def _static_recipe(recipe):
+    if recipe == "poisson":
+        sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8, 16, 32)]
+        sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
+        return D.MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
+    if recipe == "3d":
+        sx = [np.linspace(-1, 1, 5), np.linspace(-1, 1, 4), np.linspace(0, 1, 3)]
+        return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.0), (0.5, 2.0))[0]
+    return D.RectangularDecompositionND.init_params([np.array([0.5])], [np.array([1.2])], (0., 1.))[0]
+
+
+@pytest.mark.parametrize("name,recipe", [("level_params_poisson.npz", "poisson"), ("level_params_3d.npz", "3d"),
+                                         ("level_params_single.npz", "single")])
+def test_decomposition_params_match_reference(name, recipe):
+    g = golden(name)
+    st = _static_recipe(recipe)
+    p = st["subdomain"]["params"]
+    for k, nm in enumerate(["xmins", "xmaxs", "wmins", "wmaxs", "flags", "unnorms"]):
+        np.testing.assert_array_equal(p[k].numpy(), g[nm].astype(np.float32), err_msg=nm)
+    np.testing.assert_array_equal(st["subdomain"]["pou"].numpy(), g["pou"].astype(np.float32))
+    if "xmins0" in g:
+        np.testing.assert_array_equal(st["xmins0"], g["xmins0"])
+        np.testing.assert_array_equal(st["xmaxs0"], g["xmaxs0"])
+
+
+def test_non_overlapping_decomposition_rejected():
+    with pytest.raises(ValueError, match="not overlapping"):
+        D.RectangularDecompositionND.init_params([np.linspace(0, 1, 5)], [0.2 * np.ones(5)], (0., 1.))
+    with pytest.raises(ValueError, match="not same"):
+        D.RectangularDecompositionND.init_params([np.linspace(0, 1, 5)], [np.ones(4)], (0., 1.))
+
+
+def _sched_all_params(sxx, width):
+    st = D.RectangularDecompositionND.init_params(sxx, [width * np.ones_like(v) for v in sxx], (0, 1))[0]
+    return {"static": {"decomposition": st}}
+
+
+def _record(s):
+    steps, ms = [], []
+    for i, a in enumerate(s):
+        if a is not None:
+            steps.append(i)
+            ms.append(np.array(a).copy())
+    return np.array(steps), np.array(ms)
+
+
+def test_schedulers_match_reference():
+    g = golden("schedulers.npz")
+    xs1 = [np.array([-6, -4, -2, 0, 2, 4, 6.])]
+    for tag, sxx in [("1d", xs1), ("2d", xs1 * 2), ("3d", xs1 * 3)]:
+        ap = _sched_all_params(sxx, 3)
+        xd = len(sxx)
+        st, ms = _record(S.PointSchedulerRectangularND(ap, 100, np.zeros(xd)))
+        np.testing.assert_array_equal(st, g[f"point_{tag}_steps"])
+        np.testing.assert_array_equal(ms, g[f"point_{tag}_masks"])
+        if xd >= 2:
+            st, ms = _record(S.LineSchedulerRectangularND(ap, 100, np.zeros(xd - 1), 0))
+            np.testing.assert_array_equal(st, g[f"line_{tag}_steps"])
+            np.testing.assert_array_equal(ms, g[f"line_{tag}_masks"])
+        if xd >= 3:
+            st, ms = _record(S.PlaneSchedulerRectangularND(ap, 100, np.zeros(xd - 2), [0, 1]))
+            np.testing.assert_array_equal(st, g[f"plane_{tag}_steps"])
+            np.testing.assert_array_equal(ms, g[f"plane_{tag}_masks"])
+    sxb = [np.linspace(-1, 1, 16), np.linspace(0, 1, 8)]
+    apb = {"static": {"decomposition": D.RectangularDecompositionND.init_params(
+        sxb, get_subdomain_ws(sxb, 2.9), (0., 1.))[0]}}
+    st, ms = _record(S.LineSchedulerRectangularND(apb, 1000, point=[0.], iaxis=0))
+    np.testing.assert_array_equal(st, g["burgers_steps"])
+    np.testing.assert_array_equal(ms, g["burgers_masks"])
+    st, ms = _record(S.AllActiveSchedulerND(apb, 10))
+    np.testing.assert_array_equal(st, g["allactive_steps"])
+    np.testing.assert_array_equal(ms, g["allactive_masks"])
+
+
+def test_scheduler_argument_validation():
+    ap = _sched_all_params([np.array([-6, -4, -2, 0, 2, 4, 6.])] * 2, 3)
+    with pytest.raises(Exception):
+        S.PointSchedulerRectangularND(ap, 10, [0.])
+    with pytest.raises(Exception):
+        S.PlaneSchedulerRectangularND(ap, 10, [], [0, 1])
+    with pytest.raises(Exception):
+        S.LineSchedulerRectangularND(ap, 10, [0., 0.], 0)
+
+
+def test_windows_and_networks_match_reference():
+    g = golden("windows_networks.npz")
+    x = torch.tensor(g["x"])
+    lo, hi, wl, wh = (torch.tensor(g[k]) for k in ("lo", "hi", "wl", "wh"))
+    np.testing.assert_allclose(Wn.sigmoid(lo, hi, wl, wh, x).numpy(), g["win_sigmoid"], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(Wn.cosine(lo, hi, x).numpy(), g["win_cosine"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(Wn.bump(lo, hi, x).numpy(), g["win_bump"], rtol=1e-12)
+    np.testing.assert_allclose(Wn.wendland(lo, hi, x).numpy(), g["win_wendland"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(Wn.rbf(lo, hi, x).numpy(), g["win_rbf"], rtol=1e-12)
+    lay = [(torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])) for i in range(2)]
+    mk = lambda L, st=None: {"static": {"network": {"subdomain": st or {}}},
+                             "trainable": {"network": {"subdomain": {"layers": L}}}}
+    np.testing.assert_allclose(N.FCN.network_fn(mk(lay), x).numpy(), g["net_FCN"], rtol=1e-12)
+    layA = [(w, b, torch.tensor(g[f"A{i}"])) for i, (w, b) in enumerate(lay)]
+    np.testing.assert_allclose(N.AdaptiveFCN.network_fn(mk(layA), x).numpy(), g["net_AdaptiveFCN"], rtol=1e-12)
+    np.testing.assert_allclose(N.SIREN.network_fn(mk(lay), x).numpy(), g["net_SIREN"], rtol=1e-12)
+    layS = [(w, b, torch.tensor(g[f"C{i}"]), torch.tensor(g[f"O{i}"])) for i, (w, b) in enumerate(lay)]
+    np.testing.assert_allclose(N.AdaptiveSIREN.network_fn(mk(layS), x).numpy(), g["net_AdaptiveSIREN"], rtol=1e-12)
+    layF = [(torch.tensor(g["WF0"]), torch.tensor(g["bF0"])), lay[1]]
+    np.testing.assert_allclose(N.FourierFCN.network_fn(mk(layF, {"omega": torch.tensor(g["omega"])}), x).numpy(),
+                               g["net_FourierFCN"], rtol=1e-12)
+
+
+def test_network_init_distribution_and_packing():
+    _, tp = N.FCN.init_params(3, [2, 16, 16, 1])
+    for (w, b), fi in zip(tp["layers"], [2, 16, 16]):
+        v = 1 / math.sqrt(fi)
+        assert w.abs().max() <= v and b.abs().max() <= v
+    m = 5
+    layers = [(torch.randn(m, fo, fi), torch.randn(m, fo)) for fi, fo in [(2, 16), (16, 16), (16, 1)]]
+    theta = N.pack_layers(layers)
+    assert theta.shape == (m, N.fcn_param_count([2, 16, 16, 1])) == (m, 337)
+    for (w, b), (w2, b2) in zip(layers, N.unpack_layers(theta, [2, 16, 16, 1])):
+        assert torch.equal(w, w2) and torch.equal(b, b2)
+
+
+def test_grid_sampler_matches_reference():
+    """Grid order and values; values within one float32 ulp, since the fixture's
+    linspace ran in numpy float32 (the reference's jnp.linspace rounds in float32
+    its own way, this engine computes in float64 and rounds once)."""
+    g = golden("grid_sampler.npz")
+    s = DOM.RectangularDomainND._rectangle_samplerND
+    ulp = dict(rtol=0, atol=1.2e-7)
+    np.testing.assert_allclose(s(None, "grid", [0.], [1.], (200,)).numpy(), g["g1"], **ulp)
+    np.testing.assert_allclose(s(None, "grid", [-1., 0.], [1., 1.], (20, 10)).numpy(), g["g2"], **ulp)
+    np.testing.assert_allclose(s(None, "grid", [-1., -1., 0.], [1., 1., 1.], (5, 4, 3)).numpy(), g["g3"], **ulp)
+    u = s(0, "uniform", [-1., 0.], [1., 2.], (1000, 3))
+    assert u.shape == (3000, 2) and u[:, 0].min() >= -1 and u[:, 1].max() <= 2
+    assert s(None, "sobol", [0., 0.], [1., 1.], (16, 4)).shape == (64, 2)
+    assert s(None, "halton", [0.], [1.], (10,)).shape == (10, 1)
+    with pytest.raises(ValueError):
+        s(None, "bogus", [0.], [1.], (10,))
+
+
+def test_sample_boundaries_layout():
+    ps, _ = DOM.RectangularDomainND.init_params(np.array([0., 1.]), np.array([1., 2.]))
+    xb = DOM.RectangularDomainND.sample_boundaries({"static": {"domain": ps}}, 0, "grid", ((3,), (4,), (5,), (6,)))
+    assert [x.shape[0] for x in xb] == [3, 4, 5, 6]
+    assert torch.all(xb[0][:, 0] == 0) and torch.all(xb[1][:, 0] == 1)
+    assert torch.all(xb[2][:, 1] == 1) and torch.all(xb[3][:, 1] == 2)
+
+
+def test_burgers_exact_solution_matches_reference():
+    g = golden("burgers_exact.npz")
+    ap = {"static": {"problem": PR.BurgersEquation2D.init_params()[0]}}
+    u = PR.BurgersEquation2D.exact_solution(ap, torch.tensor(g["x"]), (64, 32)).double().numpy()
+    np.testing.assert_allclose(u, g["u"].astype(np.float32), rtol=0, atol=2e-6)
+
+
+def test_problem_functions_match_reference():
+    g = golden("problems.npz")
+    x, u = torch.tensor(g["x"]), torch.tensor(g["u"])
+    j = [torch.tensor(g[f"j{i}"]) for i in range(4)]
+    src = np.array([[0.1, -0.2, 0.3, 1.0], [-0.3, 0.2, 0.25, 0.5]])
+    apw = {"static": {"problem": PR.WaveEquationConstantVelocity3D.init_params(c0=1.5, source=src)[0]}}
+    apw["static"]["problem"]["source"] = torch.tensor(src)  # float64 table, as the fixture used
+    np.testing.assert_allclose(PR.WaveEquationConstantVelocity3D.constraining_fn(apw, x, u).numpy(), g["wave_c"],
+                               rtol=1e-12)
+    np.testing.assert_allclose(PR.WaveEquationConstantVelocity3D.loss_fn(apw, [[x, j[0], j[1], j[2]]]).item(),
+                               g["wave_loss"], rtol=1e-12)
+    mix = np.array([[0.2, 0.1, 0.5, 0.3], [-0.4, -0.1, 0.3, -0.2]])
+    apg = {"static": {"problem": PR.WaveEquationGaussianVelocity3D.init_params(c0=1.0, source=src, mixture=mix)[0]}}
+    apg["static"]["problem"]["mixture"] = torch.tensor(mix)
+    np.testing.assert_allclose(PR.WaveEquationGaussianVelocity3D.c_fn(apg, x).numpy(), g["wave_gauss_c_fn"],
+                               rtol=1e-12)
+    apb = {"static": {"problem": PR.BurgersEquation2D.init_params()[0]}}
+    np.testing.assert_allclose(PR.BurgersEquation2D.constraining_fn(apb, x[:, :2], u).numpy(), g["burgers_c"],
+                               rtol=1e-12)
+    aph = {"static": {"problem": PR.HarmonicOscillator1DHardBC.init_params(d=2, w0=80, sd=0.1)[0]}}
+    np.testing.assert_allclose(PR.HarmonicOscillator1DHardBC.constraining_fn(aph, x[:, :1], u).numpy(),
+                               g["hohard_c"], rtol=1e-12)
+    api = {"static": {"problem": PR.HarmonicOscillator1DInverse.init_params(d=2, w0=20)[0]}}
+    np.testing.assert_allclose(
+        PR.HarmonicOscillator1DInverse.exact_solution(api, torch.linspace(0, 1, 13, dtype=torch.float64)
+                                                      .reshape(13, 1)).numpy(), g["ho_inv_data"], rtol=1e-12)
+
+
+def test_poisson_manufactured_solution_consistent():
+    """-lap of the manufactured u equals the source f (central differences)."""
+    ap = {"static": {"problem": PR.Poisson2D.init_params()[0]}}
+    x = torch.rand(50, 2, dtype=torch.float64) * 0.8 + 0.1
+    h = 1e-4
+    lap = 0
+    for d in range(2):
+        e = torch.zeros(1, 2, dtype=torch.float64)
+        e[0, d] = h
+        u = lambda z: PR.Poisson2D.exact_solution(ap, z).double()
+        lap = lap + (u(x + e) - 2 * u(x) + u(x - e)) / h ** 2
+    f = PR.Poisson2D.source(ap, x)
+    assert torch.allclose(-lap, f, rtol=0, atol=1e-4 * f.abs().max().item())
+
+
+def test_cell_grid_registers_every_containing_box():
+    """Monotone cell lookup: every box containing a point is in the point's cell list."""
+    rng = np.random.default_rng(0)
+    xmin = rng.uniform(0, 1, (300, 2)).astype(np.float32)
+    xmax = (xmin + rng.uniform(0.01, 0.3, (300, 2))).astype(np.float32)
+    g = D.build_cell_grid(xmin, xmax)
+    x = np.concatenate([rng.uniform(-0.1, 1.4, (5000, 2)), xmin, xmax]).astype(np.float32)
+    cells = [D.cell_coord(x[:, d], g["lo"][d], g["inv_h"][d], g["ncell"][d]) for d in range(2)]
+    cid = cells[0] + g["ncell"][0] * cells[1]
+    inside = np.all((x[:, None, :] >= xmin[None]) & (x[:, None, :] <= xmax[None]), -1)
+    for p in range(x.shape[0]):
+        cand = set(g["cell_boxes"][g["cell_start"][cid[p]]:g["cell_start"][cid[p] + 1]].tolist())
+        assert set(np.nonzero(inside[p])[0].tolist()) <= cand
+    # boxes ascending within every cell
+    for c in range(len(g["cell_start"]) - 1):
+        seg = g["cell_boxes"][g["cell_start"][c]:g["cell_start"][c + 1]]
+        assert np.all(np.diff(seg) > 0)
+
+
+def test_constants_key_checking_and_defaults():
+    c = Constants(n_steps=3)
+    assert c.n_steps == 3 and c["sampler"] == "grid"
+    with pytest.raises(KeyError):
+        c["nonexistent"] = 1
+    with pytest.raises(KeyError):
+        Constants(nonexistent=1)
+    assert [float(v) for v in get_subdomain_ws([np.linspace(0, 1, 5)], 2.0)[0]] == [0.5] * 5
+
+
+def test_library_exports_every_declared_symbol():
+    """libfbpgpu.so loads without a GPU and exports every entry point of include/fbpgpu.h."""
+    from fbpinns_gb300 import _lib
+    lib = _lib.load()
+    declared = _lib.declared_symbols()
+    assert len(declared) >= 20
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(declared) <= set(_lib._SIG), set(declared) - set(_lib._SIG)
+    assert lib.fbp_abi_version() == 1
+
+
+def test_required_ujs_mapping():
+    from fbpinns_gb300.engine import d2mask_of, jet_index, jet_size
+    assert d2mask_of([((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0)))], 2) == 1
+    assert d2mask_of([((0, (0, 0)), (0, (1, 1)), (0, (2, 2)))], 3) == 7
+    assert jet_size(3, 7) == 7 and jet_index(3, 7, (2, 2)) == 6 and jet_index(2, 2, (1, 1)) == 3
+    with pytest.raises(NotImplementedError):
+        d2mask_of([((0, (0, 1)),)], 2)
+    with pytest.raises(NotImplementedError):
+        d2mask_of([((0, (0, 0, 0)),)], 1)
