@@ -56,6 +56,10 @@ __host__ __device__ constexpr int nth_bit(int mask, int s) {
     return 0;
 }
 
+// Row stride (floats) of the per-pair and per-slot jet records [first J | second J]:
+// 2J rounded up to a multiple of 4 so that rows can be moved as float4.
+__host__ __device__ constexpr int rec_stride(int J) { return (2 * J + 3) / 4 * 4; }
+
 // Compile-time table of the set bits of a mask (up to 3): DimsOf<M>::get(s) is
 // the s-th set bit, folded to a constant when s is a constant.
 template <int M>

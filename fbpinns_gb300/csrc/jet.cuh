@@ -260,8 +260,9 @@ __device__ __forceinline__ void net_jet(const SParams<C>& S, const float (&xn)[C
 constexpr int FWD_THREADS = 128;
 
 template <class C>
-__global__ void __launch_bounds__(FWD_THREADS) forward_pairs_kernel(fbp_net net, const float* __restrict__ x,
+__global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net net, const float* __restrict__ x,
                                                                      fbp_pairs pr, float* __restrict__ pair_out) {
+    constexpr int J = C::J, XD = C::XD, RS = rec_stride(C::J);
     __shared__ SParams<C> S;
     __shared__ float a1s[C::H1 * FWD_THREADS];
     const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
@@ -269,36 +270,56 @@ __global__ void __launch_bounds__(FWD_THREADS) forward_pairs_kernel(fbp_net net,
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
         load_params<C>(S, net, j);
-        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-            const int e = beg + t;
-            const int pt = pr.sd_point[e];
-            const int pos = pr.sd_pair[e];
-            float xn[C::XD];
-            load_point<C>(S, x, pt, xn);
-            float o[C::J];
+        // software pipeline: the next pair's indices and coordinates are loaded
+        // while the current pair is computed
+        int t = threadIdx.x;
+        int pos_n = 0;
+        float xr_n[XD];
+#pragma unroll
+        for (int d = 0; d < XD; ++d) xr_n[d] = 0.f;
+        if (t < cnt) {
+            const int pt = pr.sd_point[beg + t];
+            pos_n = pr.sd_pair[beg + t];
+#pragma unroll
+            for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+        }
+        for (; t < cnt; t += blockDim.x) {
+            const int pos = pos_n;
+            float xn[XD];
+#pragma unroll
+            for (int d = 0; d < XD; ++d) xn[d] = (xr_n[d] - S.mu[d]) * S.inv_sd[d];
+            const int tn = t + blockDim.x;
+            if (tn < cnt) {
+                const int pt = pr.sd_point[beg + tn];
+                pos_n = pr.sd_pair[beg + tn];
+#pragma unroll
+                for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+            }
+            float o[J];
             net_jet<C>(S, xn, &a1s[threadIdx.x], FWD_THREADS, o);
             // unnormalisation (decompositions.py:191-194): u = u_raw*sd + mu
-            float u[C::J];
+            float u[J];
 #pragma unroll
-            for (int c = 0; c < C::J; ++c) u[c] = o[c] * S.sd_u;
+            for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
             u[0] += S.mu_u;
-            float w[C::J];
+            float w[J];
             window_jet<C>(S, xn, w);
-            float uw[C::J];
-            uw[0] = u[0] * w[0];
+            float rec[RS];
+            rec[0] = u[0] * w[0];
 #pragma unroll
-            for (int d = 0; d < C::XD; ++d) uw[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
+            for (int d = 0; d < XD; ++d) rec[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
 #pragma unroll
             for (int s = 0; s < C::NS; ++s) {
                 const int d = C::sd_dim(s);
-                uw[1 + C::XD + s] = u[1 + C::XD + s] * w[0] + 2.0f * u[1 + d] * w[1 + d] + u[0] * w[1 + C::XD + s];
+                rec[1 + XD + s] = u[1 + XD + s] * w[0] + 2.0f * u[1 + d] * w[1 + d] + u[0] * w[1 + XD + s];
             }
-            float* dst = pair_out + (size_t)pos * (2 * C::J);
 #pragma unroll
-            for (int c = 0; c < C::J; ++c) {
-                dst[c] = uw[c];
-                dst[C::J + c] = w[c];
-            }
+            for (int c = 0; c < J; ++c) rec[J + c] = w[c];
+#pragma unroll
+            for (int c = 2 * J; c < RS; ++c) rec[c] = 0.f;
+            float4* dst = reinterpret_cast<float4*>(pair_out + (size_t)pos * RS);
+#pragma unroll
+            for (int q = 0; q < RS / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
         }
     }
 }
@@ -412,9 +433,22 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                 float w[J];
                 window_jet<C>(S, xn, w);
                 float nb[J];
-                const bool ok = slot >= 0 && slot < pr.slots_cap;  // overflowed slots carry no seed
+                {
+                    constexpr int RS = rec_stride(J);
+                    const bool ok = slot >= 0 && slot < pr.slots_cap;  // overflowed slots carry no seed
+                    float rec[(J + 3) / 4 * 4];
+                    const float4* src = reinterpret_cast<const float4*>(slot_out + (size_t)(ok ? slot : 0) * RS);
 #pragma unroll
-                for (int c = 0; c < J; ++c) nb[c] = ok ? slot_out[(size_t)slot * (2 * J) + c] : 0.f;
+                    for (int q = 0; q < (J + 3) / 4; ++q) {
+                        const float4 v = src[q];
+                        rec[4 * q] = v.x;
+                        rec[4 * q + 1] = v.y;
+                        rec[4 * q + 2] = v.z;
+                        rec[4 * q + 3] = v.w;
+                    }
+#pragma unroll
+                    for (int c = 0; c < J; ++c) nb[c] = ok ? rec[c] : 0.f;
+                }
                 // adjoint of uw = u (*) w with w constant: u-bar = M_w^T N-bar
                 float ub[J];
                 ub[0] = nb[0] * w[0];

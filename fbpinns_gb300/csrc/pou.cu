@@ -275,6 +275,7 @@ constexpr int POU_T = 256;
 template <int XD, int D2>
 struct PointPOU {
     static constexpr int J = JL<XD, D2>::J;
+    static constexpr int RS = rec_stride(J);  // row stride of pair and slot records
     // forward POU for point p; writes slot records; returns U (unconstrained)
     __device__ static void run(int64_t p, int npou, const int32_t* __restrict__ pt_off,
                                const int32_t* __restrict__ p_take, const float* __restrict__ pair_out,
@@ -293,7 +294,7 @@ struct PointPOU {
 #pragma unroll
                     for (int c = 0; c < J; ++c) U[c] += Ul[c];
                     if (cur < u_cap) {
-                        float* so = slot_out + (size_t)cur * (2 * J);
+                        float* so = slot_out + (size_t)cur * RS;
 #pragma unroll
                         for (int c = 0; c < J; ++c) {
                             so[c] = Ul[c];
@@ -307,11 +308,20 @@ struct PointPOU {
                 for (int c = 0; c < J; ++c) N[c] = W[c] = 0.f;
             }
             if (e < e1) {
-                const float* po = pair_out + (size_t)e * (2 * J);
+                const float4* po = reinterpret_cast<const float4*>(pair_out + (size_t)e * RS);
+                float rec[RS];
+#pragma unroll
+                for (int q = 0; q < RS / 4; ++q) {
+                    const float4 v = po[q];
+                    rec[4 * q] = v.x;
+                    rec[4 * q + 1] = v.y;
+                    rec[4 * q + 2] = v.z;
+                    rec[4 * q + 3] = v.w;
+                }
 #pragma unroll
                 for (int c = 0; c < J; ++c) {
-                    N[c] += po[c];
-                    W[c] += po[J + c];
+                    N[c] += rec[c];
+                    W[c] += rec[J + c];
                 }
             }
         }
@@ -329,7 +339,7 @@ struct PointPOU {
         for (int c = 0; c < J; ++c) ubl[c] = Ub[c] * inv;
         const int u1 = (int)min((int64_t)np_off[p + 1], u_cap);
         for (int u = np_off[p]; u < u1; ++u) {
-            float* so = slot_out + (size_t)u * (2 * J);
+            float* so = slot_out + (size_t)u * RS;
             float W[J], Nb[J];
 #pragma unroll
             for (int c = 0; c < J; ++c) W[c] = so[J + c];

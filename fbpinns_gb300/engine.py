@@ -76,6 +76,11 @@ def jet_size(xd, d2mask):
     return 1 + xd + bin(d2mask).count("1")
 
 
+def record_stride(J):
+    """Row stride (floats) of the pair / slot jet records: 2J rounded up to 4."""
+    return (2 * J + 3) // 4 * 4
+
+
 class PointSet:
     """Interaction lists, subdomain-major pair order, work queues and jet buffers
     of one set of points ``x`` (n, xd) on the device.
@@ -121,8 +126,9 @@ class PointSet:
         self.item_start_act = torch.zeros(m + 1, **i32)
         self.n_items_all = torch.zeros(1, **i32)
         self.n_items_act = torch.zeros(1, **i32)
-        self.pair_out = torch.empty((max(s_cap, 1), 2 * self.J), dtype=torch.float32, device=dev)
-        self.slot_out = torch.empty((max(u_cap, 1), 2 * self.J), dtype=torch.float32, device=dev)
+        R = record_stride(self.J)
+        self.pair_out = torch.empty((max(s_cap, 1), R), dtype=torch.float32, device=dev)
+        self.slot_out = torch.empty((max(u_cap, 1), R), dtype=torch.float32, device=dev)
         self.grad_part = torch.empty((self.items_cap, eng.P), dtype=torch.float32, device=dev)
         self.U = torch.empty((self.n, self.J), dtype=torch.float32, device=dev)
         self._sized = True

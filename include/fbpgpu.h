@@ -27,6 +27,10 @@
  * J = 1 + xd + popcount(d2).  This is the per-point set of derivative jets
  * that the reference obtains from nested forward-mode jvp
  * (fbpinns/trainers.py:213-247, _get_ujs / jacfwd).
+ *
+ * Per-pair and per-slot jet records ([first J values | second J values]) are
+ * rows of R = 2J rounded up to a multiple of 4 floats (16-byte rows):
+ * pair_out is (s, R) and slot_out is (u, R), both 16-byte aligned.
  */
 #ifndef FBPGPU_H
 #define FBPGPU_H
@@ -213,7 +217,7 @@ int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t* select, in
                    int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
 
 /* Per-pair forward jets: for every pair in the work items, the jets of
- * u_j(x) * w_j(x) and of w_j(x) (J + J floats at pair_out[pair*2J]), where
+ * u_j(x) * w_j(x) and of w_j(x) (J + J floats in row `pair` of pair_out), where
  * u_j = unnorm(FCN_j(norm(x))) and w_j is the cosine window.
  * Replaces the vmapped FBPINN_model_inner under nested jvp
  * (fbpinns/trainers.py:113-118,158, 219-227; networks.py:61-68;
