@@ -43,3 +43,17 @@ extern "C" int fbp_adjoint_pairs(const fbp_net* net, const float* x, const fbp_p
     FBP_REQUIRE(slot_out, FBP_ERR_INVALID, "fbp_adjoint_pairs: null slot_out");
     return fbp::dispatch(1, net, x, pairs, slot_out, grad_part, grid, stream);
 }
+
+extern "C" int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask) {
+    fbp_net net{};
+    net.xd = xd;
+    net.h1 = h1;
+    net.h2 = h2;
+    net.ud = 1;
+    net.d2mask = d2mask;
+    fbp_pairs pr{};
+    int r = fbp::jet_group_a(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
+    if (r == 1) r = fbp::jet_group_b(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
+    if (r == 1) r = fbp::jet_group_c(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
+    return r == FBP_OK ? 1 : 0;
+}

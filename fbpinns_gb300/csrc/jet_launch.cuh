@@ -56,6 +56,7 @@ template <int XD, int H1, int H2, int D2>
 int try_shape(int mode, const fbp_net& net, const float* x, const fbp_pairs& pr, const float* slot_out, float* out,
               int grid, cudaStream_t st) {
     if (net.xd != XD || net.h1 != H1 || net.h2 != H2 || net.d2mask != D2) return 1;
+    if (mode == 2) return FBP_OK;  // shape query: compiled
     if (mode == 0) return launch_forward<XD, H1, H2, D2>(net, x, pr, out, grid, st);
     return launch_adjoint<XD, H1, H2, D2>(net, x, pr, slot_out, out, grid, st);
 }

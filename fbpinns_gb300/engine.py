@@ -216,6 +216,10 @@ class FBPINNEngine:
         self.h2 = ls[2] if len(ls) == 4 else 0
         self.P = fcn_param_count(ls)
         self.d2mask = int(d2mask)
+        if not _lib.load().fbp_has_shape(self.xd, self.h1, self.h2, self.d2mask):
+            raise _lib.FBPLibraryError(
+                f"no compiled jet kernels for layer sizes {ls} with second derivatives along dims "
+                f"{[d for d in range(self.xd) if (self.d2mask >> d) & 1]}; add the shape to csrc/jet_inst_*.cu")
         self.J = jet_size(self.xd, self.d2mask)
         self.chunk = int(chunk)
         self.launch_grid = int(grid) if grid else 0
@@ -422,3 +426,15 @@ def constrained_jets(cfn, all_params, x, U, xd, d2mask):
 
             out[1 + d] = torch.func.jvp(h, (zero,), (ones,))[1]
     return torch.cat(out, dim=1)
+
+
+def inference_d2mask(layer_sizes):
+    """A compiled jet mask for value-only evaluation of this network shape."""
+    lib = _lib.load()
+    xd = layer_sizes[0]
+    h1 = layer_sizes[1]
+    h2 = layer_sizes[2] if len(layer_sizes) == 4 else 0
+    for mask in range(1 << xd):
+        if lib.fbp_has_shape(xd, h1, h2, mask):
+            return mask
+    raise _lib.FBPLibraryError(f"no compiled jet kernels for layer sizes {list(layer_sizes)}")

@@ -161,13 +161,20 @@ class FusedStep:
                               eps_root=o["eps_root"])
 
     def capture(self, warmup=2):
-        """Capture one step in a CUDA graph (after ``warmup`` eager steps on a side stream)."""
+        """Capture one step in a CUDA graph after ``warmup`` eager steps on a side
+        stream; the warm-up steps' updates (parameters, Adam moments, step count,
+        hence also the sampler's stream offset) are rolled back, so capturing does
+        not advance training."""
+        eng = self.eng
+        saved = [t.clone() for t in (eng.theta, eng.m1, eng.m2, eng.count)]
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
             for _ in range(warmup):
                 self._body()
         torch.cuda.current_stream().wait_stream(s)
+        for dst, src in zip((eng.theta, eng.m1, eng.m2, eng.count), saved):
+            dst.copy_(src)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self._body()
@@ -260,12 +267,16 @@ class FBPINNTrainer:
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()
         all_params["static"]["problem"] = {k: _to_dev(v, dev) for k, v in all_params["static"]["problem"].items()}
         opt = c.optimiser(**c.optimiser_kwargs)
+        if c.engine not in ("fused", "generic", "plain"):
+            raise ValueError(f"engine must be 'fused', 'generic' or 'plain', not {c.engine!r}")
         spec = problem.fused_spec(all_params) if c.engine == "fused" else None
-        use_fused = (spec is not None and len(constraints_global) == 1
-                     and not all_params["trainable"].get("problem"))
-        if c.resample and not use_fused:
-            raise NotImplementedError("resampling per step is implemented for the fused built-in problems")
-
+        single = len(constraints_global) == 1 and not all_params["trainable"].get("problem")
+        use_fused = spec is not None and single
+        use_plain = c.engine == "plain"
+        if use_plain and not single:
+            raise NotImplementedError("the plain step handles one constraint without trainable problem params")
+        if c.resample and not (use_fused or use_plain):
+            raise NotImplementedError("per-step resampling is implemented for the fused and plain steps")
         # test data (fbpinns/trainers.py:463-470, 620-624)
         x_test = domain.sample_interior(all_params, None, "grid", c.n_test)
         u_exact = problem.exact_solution(all_params, x_test, c.n_test)
@@ -308,19 +319,20 @@ class FBPINNTrainer:
                     has = np.ones(m, dtype=bool)
                 state = state * has
                 eng.set_state(state)
+                res = None
+                if c.resample:
+                    d = all_params["static"]["domain"]
+                    res = (int(np.prod(c.ns[0])), d["xmin"].tolist(), d["xmax"].tolist(), c.seed)
                 if use_fused:
-                    if step is None:
-                        res = None
-                        if c.resample:
-                            d = all_params["static"]["domain"]
-                            res = (int(np.prod(c.ns[0])), d["xmin"].tolist(), d["xmax"].tolist(), c.seed)
+                    if step is not None and training_x is None:
+                        step.set_state(state)
+                    else:
                         step = FusedStep(eng, spec, opt, x=training_x, resample=res, use_graph=c.use_graph,
                                          headroom=c.pair_headroom)
-                    else:
-                        if training_x is not None:
-                            step = FusedStep(eng, spec, opt, x=training_x, use_graph=c.use_graph)
-                        else:
-                            step.set_state(state)
+                elif use_plain:
+                    from .plain import PlainStep
+                    step = PlainStep(eng, problem, all_params, required[0], opt, x=training_x, resample=res,
+                                     headroom=c.pair_headroom)
                 else:
                     step = GenericStep(eng, problem, all_params, cons, required)
                 logger.info(f"[i: {i}/{c.n_steps}] Updating active inputs done ({time.time() - t0:.2f} s)")
@@ -350,6 +362,17 @@ class FBPINNTrainer:
         logger.info(f"[i: {c.n_steps}/{c.n_steps}] Training complete")
         return all_params
 
+    @staticmethod
+    def _numpy_tree(d):
+        """Copy of a params tree with tensors as numpy arrays and private keys dropped."""
+        if isinstance(d, dict):
+            return {k: FBPINNTrainer._numpy_tree(v) for k, v in d.items() if not str(k).startswith("_")}
+        if isinstance(d, (list, tuple)):
+            return type(d)(FBPINNTrainer._numpy_tree(v) for v in d)
+        if torch.is_tensor(d):
+            return d.detach().cpu().numpy().copy()
+        return d
+
     def model_tuple(self, i, eng, all_params):
         """(i, all_params, all_opt_states, active, u_test_losses) as numpy, the
         layout of the reference's model pickles (fbpinns/trainers.py:721)."""
@@ -357,7 +380,9 @@ class FBPINNTrainer:
         layers = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.theta, ls)]
         mu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m1, ls)]
         nu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m2, ls)]
-        ap = {"static": all_params["static"], "trainable": {"network": {"subdomain": {"layers": layers}}}}
+        ap = {"static": self._numpy_tree(all_params["static"]),
+              "trainable": {"network": {"subdomain": {"layers": layers}},
+                            **{k: self._numpy_tree(v) for k, v in all_params["trainable"].items() if k != "network"}}}
         opt = {"count": int(eng.count.item()), "mu": {"network": {"subdomain": {"layers": mu}}},
                "nu": {"network": {"subdomain": {"layers": nu}}}}
         return (i, ap, opt, eng.state.cpu().numpy().astype(int), np.array(self.u_test_losses))
@@ -386,3 +411,31 @@ class FBPINNTrainer:
             eng.forward_pairs(ps)
             U = eng.pou_forward(ps)
             return problem.constraining_fn(all_params, x, U[:, 0:1])
+
+
+class PINNTrainer(FBPINNTrainer):
+    """A single network over the whole domain (fbpinns/trainers.py:780-943).
+
+    Run as the m = 1 case of the FBPINN engine: one box equal to the domain,
+    so the subdomain normalisation is the domain's ``norm_fn``, the window flag
+    is 0 (w = 1), the POU sum is the network output, and the unnormalisation
+    uses ``decomposition_init_kwargs["unnorm"]`` as the reference's PINN does.
+    """
+
+    def train(self):
+        from .decompositions import RectangularDecompositionND
+        from .schedulers import AllActiveSchedulerND
+        c = self.c
+        lo = np.asarray(c.domain_init_kwargs["xmin"], dtype=np.float64)
+        hi = np.asarray(c.domain_init_kwargs["xmax"], dtype=np.float64)
+        unnorm = c.decomposition_init_kwargs.get("unnorm", (0., 1.))
+        saved = (c.decomposition, c.decomposition_init_kwargs, c.scheduler, c.scheduler_kwargs)
+        c.decomposition = RectangularDecompositionND
+        c.decomposition_init_kwargs = dict(subdomain_xs=[np.array([(a + b) / 2]) for a, b in zip(lo, hi)],
+                                           subdomain_ws=[np.array([b - a]) for a, b in zip(lo, hi)],
+                                           unnorm=unnorm)
+        c.scheduler, c.scheduler_kwargs = AllActiveSchedulerND, {}
+        try:
+            return super().train()
+        finally:
+            c.decomposition, c.decomposition_init_kwargs, c.scheduler, c.scheduler_kwargs = saved

@@ -225,6 +225,10 @@ int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t* select, in
 int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs,
                       float* pair_out, int32_t grid, void* stream);
 
+/* 1 if the per-pair jet kernels are compiled for this network shape and jet
+ * mask (ud = 1), else 0.  Lets a caller fail early with a clear message. */
+int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask);
+
 /* POU combination per point (the two segment sums and the divide of
  * fbpinns/trainers.py:162-170, on jets by the quotient rule):
  *   slot_out[u] = (U_l jets, W_l jets) of each (point, level) slot,

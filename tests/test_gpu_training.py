@@ -1,0 +1,79 @@
+"""Training runs on the GPU: every workload configuration (reduced sizes)
+through FBPINNTrainer, matched test error of the fused and plain steps, the
+PINN trainer, and model save / load in the reference's pickle layout."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from fbpinns_gb300 import configs
+from fbpinns_gb300.trainers import FBPINNTrainer, PINNTrainer
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,steps", [("ho", 300), ("burgers", 300), ("poisson", 200), ("wave", 60),
+                                        ("helmholtz", 60)])
+def test_config_trains(cuda, name, steps):
+    c = configs.CONFIGS[name](n_steps=steps, small=True)
+    c.summary_freq = max(1, steps // 6)
+    c.test_freq = steps
+    tr = FBPINNTrainer(c)
+    tr.train()
+    losses = [h["loss"] for h in tr.history]
+    assert all(math.isfinite(v) for v in losses)
+    l1 = [r[1] for r in tr.u_test_losses]
+    assert len(l1) == 2 and all(math.isfinite(v) for v in l1)
+    if name in ("ho", "poisson", "burgers"):
+        assert losses[-1] < losses[0]
+
+
+def test_matched_test_error_fused_vs_plain(cuda):
+    """Same initial parameters and the same per-step points (Philox stream keyed
+    by the step count): the fused and the plain step reach the same test L1."""
+    res = {}
+    for engine in ("fused", "plain"):
+        c = configs.poisson(n_steps=120, small=True)
+        c.engine = engine
+        c.summary_freq, c.test_freq = 40, 120
+        tr = FBPINNTrainer(c)
+        tr.train()
+        res[engine] = (tr.u_test_losses[-1][1], [h["loss"] for h in tr.history])
+    l1f, l1p = res["fused"][0], res["plain"][0]
+    assert abs(l1f - l1p) <= 0.05 * l1p, (l1f, l1p)
+    for a, b in zip(res["fused"][1], res["plain"][1]):
+        assert abs(a - b) <= 0.05 * abs(b)
+
+
+def test_pinn_trainer(cuda):
+    c = configs.ho(n_steps=200)
+    c.network_init_kwargs = dict(layer_sizes=[1, 32, 32, 1])
+    c.summary_freq, c.test_freq = 50, 200
+    tr = PINNTrainer(c)
+    ap = tr.train()
+    assert tr.engine.m == 1
+    assert float(tr.engine.grid.flags[0]) == 0.0
+    losses = [h["loss"] for h in tr.history]
+    assert losses[-1] < losses[0]
+
+
+def test_model_save_and_load(cuda, tmp_path, monkeypatch):
+    from fbpinns_gb300.analysis import load_model, FBPINN_solution
+    monkeypatch.chdir(tmp_path)
+    c = configs.ho(n_steps=20)
+    c.run = "saved"
+    c.save_models = True
+    c.model_save_freq = 20
+    c.summary_freq, c.test_freq = 10, 20
+    tr = FBPINNTrainer(c)
+    tr.train()
+    c2, model = load_model("saved", rootdir="results/")
+    i, all_params, opt, active, losses = model
+    assert i == 20 and opt["count"] == 20 and active.shape == (15,)
+    x = torch.linspace(0, 1, 50).reshape(-1, 1)
+    u_loaded = FBPINN_solution(c2, all_params, active, x)
+    u_live = FBPINNTrainer.predict(tr.engine, tr.all_params, c.problem, x)
+    assert torch.allclose(u_loaded, u_live, rtol=1e-6, atol=1e-6)
