@@ -58,14 +58,14 @@ def poisson(n_steps=10000, small=False):
     levels = [1, 2, 4, 8] if small else [1, 2, 4, 8, 16, 32]
     sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in levels[1:]]
     sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
-    n = 1 << 14 if small else 1 << 18
+    n = (128, 128) if small else (512, 512)  # 2^14 / 2^18 points
     return Constants(run="poisson", domain=domains.RectangularDomainND,
                      domain_init_kwargs=dict(xmin=np.array([0., 0.]), xmax=np.array([1., 1.])),
                      problem=problems.Poisson2D, problem_init_kwargs=dict(n_freq=4 if small else 6, sd=0.1),
                      decomposition=decompositions.MultilevelRectangularDecompositionND,
                      decomposition_init_kwargs=dict(subdomain_xss=sxs, subdomain_wss=sws, unnorm=(0., 1.)),
                      network=networks.FCN, network_init_kwargs=dict(layer_sizes=[2, 16, 16, 1]),
-                     ns=((n,),), sampler="uniform", resample=True, n_test=(100, 100), n_steps=n_steps,
+                     ns=(n,), sampler="uniform", resample=True, n_test=(100, 100), n_steps=n_steps,
                      optimiser_kwargs=dict(learning_rate=1e-3),
                      summary_freq=max(1, n_steps // 10), test_freq=max(1, n_steps // 5))
 
@@ -96,7 +96,7 @@ def helmholtz(n_steps=10000, small=False):
     2.9x spacing), FCN 2-32-32-1, 2^22 uniform points redrawn every step."""
     k = 16 if small else 64
     sx = [np.linspace(0, 1, k)] * 2
-    n = 1 << 16 if small else 1 << 22
+    n = (256, 256) if small else (2048, 2048)  # 2^16 / 2^22 points
     return Constants(run="helmholtz", domain=domains.RectangularDomainND,
                      domain_init_kwargs=dict(xmin=np.array([0., 0.]), xmax=np.array([1., 1.])),
                      problem=problems.Helmholtz2D,
@@ -105,7 +105,7 @@ def helmholtz(n_steps=10000, small=False):
                      decomposition_init_kwargs=dict(subdomain_xs=sx, subdomain_ws=get_subdomain_ws(sx, 2.9),
                                                     unnorm=(0., 1.)),
                      network=networks.FCN, network_init_kwargs=dict(layer_sizes=[2, 32, 32, 1]),
-                     ns=((n,),), sampler="uniform", resample=True, n_test=(200, 200), n_steps=n_steps,
+                     ns=(n,), sampler="uniform", resample=True, n_test=(200, 200), n_steps=n_steps,
                      optimiser_kwargs=dict(learning_rate=1e-3),
                      summary_freq=max(1, n_steps // 10), test_freq=max(1, n_steps // 5))
 
