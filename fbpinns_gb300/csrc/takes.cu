@@ -68,6 +68,10 @@ __global__ void inside_count_kernel(const float* __restrict__ x, int64_t n, fbp_
     }
 }
 
+// One warp per point: the lanes test 32 consecutive candidates of the point's
+// cell at a time (candidates ascend by box id) and write the hits at
+// ballot-ranked consecutive positions, so each point's pairs are written
+// coalesced and in ascending box order.
 template <int XD>
 __global__ void inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b,
                                    const int32_t* __restrict__ pt_off, const int32_t* __restrict__ np_off,
@@ -75,8 +79,10 @@ __global__ void inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_b
                                    int32_t* __restrict__ m_take, int32_t* __restrict__ p_take,
                                    int32_t* __restrict__ np_take, int64_t s_cap, int64_t u_cap,
                                    int32_t* __restrict__ status) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-         p += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp; p < n; p += nwarps) {
         float xp[XD];
 #pragma unroll
         for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
@@ -85,35 +91,38 @@ __global__ void inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_b
         const uint64_t lvl = pt_lvl[p];
         const int64_t base = pt_off[p];
         const int64_t ubase = np_off[p];
-        int k = 0;
-        for (int e = e0; e < e1; ++e) {
-            const int j = b.cell_boxes[e];
-            if (b.select && !b.select[j]) continue;
-            if (inside_box<XD>(xp, b.xmins, b.xmaxs, j)) {
-                const int64_t o = base + k;
-                ++k;
-                if (o >= s_cap) {
-                    atomicOr(status, FBP_STATUS_PAIR_OVERFLOW);
-                    continue;
-                }
-                const int lv = b.pou[j] & 63;
-                const uint64_t below = lv ? (lvl & ((1ull << lv) - 1ull)) : 0ull;
-                n_take[o] = (int32_t)p;
-                m_take[o] = j;
-                p_take[o] = (int32_t)(ubase + __popcll(below));
+        int64_t k = 0;
+        for (int e = e0; e < e1; e += 32) {
+            const int ee = e + lane;
+            int j = -1;
+            bool hit = false;
+            if (ee < e1) {
+                j = b.cell_boxes[ee];
+                hit = (!b.select || b.select[j]) && inside_box<XD>(xp, b.xmins, b.xmaxs, j);
             }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int64_t o = base + k + __popc(m & ((1u << lane) - 1u));
+                if (o < s_cap) {
+                    const int lv = b.pou[j] & 63;
+                    const uint64_t below = lv ? (lvl & ((1ull << lv) - 1ull)) : 0ull;
+                    n_take[o] = (int32_t)p;
+                    m_take[o] = j;
+                    p_take[o] = (int32_t)(ubase + __popcll(below));
+                } else {
+                    atomicOr(status, FBP_STATUS_PAIR_OVERFLOW);
+                }
+            }
+            k += __popc(m);
         }
-        // unique (point, level) slots in ascending level order
-        uint64_t bits = lvl;
-        int r = 0;
-        while (bits) {
+        // unique (point, level) slots in ascending level order: lane r writes slots r, r+32
+        const int nl = __popcll(lvl);
+        for (int r = lane; r < nl; r += 32) {
             const int64_t o = ubase + r;
             if (o < u_cap)
                 np_take[o] = (int32_t)p;
             else
                 atomicOr(status, FBP_STATUS_SLOT_OVERFLOW);
-            bits &= bits - 1ull;
-            ++r;
         }
     }
 }
@@ -425,7 +434,7 @@ extern "C" int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes
     FBP_REQUIRE((n_take && m_take && p_take) || s_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null take");
     FBP_REQUIRE(np_take || u_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null np_take");
     if (n == 0) return FBP_OK;
-    const int g = grid_for(n, 256);
+    const int g = grid_for(n * 32, 256, 8);  // one warp per point
     cudaStream_t st = as_stream(stream);
     switch (boxes->xd) {
         case 1: inside_fill_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
