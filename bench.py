@@ -236,7 +236,8 @@ def run_fused(args, world, rank, local):
     opt = adam(LR)
     seed = SEED + 1000 * rank
 
-    eng = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid)
+    tc = False if args.fma_forward else None
+    eng = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
@@ -272,7 +273,7 @@ def run_fused(args, world, rank, local):
     # ---- end to end through the public step API with host buffers ----------
     e2e = None
     try:
-        eng2 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid)
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -319,6 +320,10 @@ def run_fused(args, world, rank, local):
 
     timed("takes_sort_work", lambda: ps.rebuild())
     timed("forward_pairs", lambda: eng.forward_pairs(ps))
+    if eng.tensor_cores:  # the CUDA-core FMA forward on the same pairs, for comparison
+        eng.tensor_cores = False
+        timed("forward_pairs_fma", lambda: eng.forward_pairs(ps))
+        eng.tensor_cores = True
     timed("pou_loss", lambda: eng.pou_loss(ps))
     timed("adjoint_pairs", lambda: eng.adjoint(ps, reduce=False))
     timed("grad_reduce", lambda: eng.reduce_grad(ps))
@@ -393,6 +398,7 @@ def run_fused(args, world, rank, local):
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
                            "parallelism": f"replicas x{world}", "chunk": args.chunk,
+                           "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
                                  ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
                 "e2e": e2e, "gpu_launches": per_step * args.steps, "clocks": clocks, "roofline": roofline,
@@ -409,6 +415,7 @@ def main():
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
     ap.add_argument("--chunk", type=int, default=512)
     ap.add_argument("--grid", type=int, default=0)
+    ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-timed", action="store_true",

@@ -19,6 +19,7 @@ STATUS_BITS = {
     4: "work-item overflow",
     8: "a point's POU levels are not in ascending subdomain order",
     16: "index out of range",
+    32: "tensor-core kernel timed out waiting for its MMAs",
 }
 
 PROBLEM_NONE, PROBLEM_HO_HARDBC, PROBLEM_BURGERS, PROBLEM_POISSON2D, PROBLEM_WAVE_C, PROBLEM_HELMHOLTZ2D = range(6)
@@ -69,6 +70,7 @@ _SIG = {
     "fbp_work_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_build_work": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, C.c_size_t, _P]),
     "fbp_forward_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _I32, _P]),
+    "fbp_forward_pairs_tc": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _P, _I32, _P]),
     "fbp_pou_forward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _P]),
     "fbp_pou_backward": (C.c_int, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _P]),
     "fbp_pou_loss": (C.c_int, [_I32, _I32, C.POINTER(Problem), _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _I64, _I64,

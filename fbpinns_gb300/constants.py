@@ -104,6 +104,7 @@ class Constants(ConstantsBase):
         self.chunk = 512               # pairs per work item
         self.launch_grid = 0           # CTAs of the persistent jet kernels (0 = 4 per SM)
         self.use_graph = True          # capture the step in a CUDA graph
+        self.tensor_cores = None       # forward jets on tcgen05 (3xTF32): None = where compiled, True, False
         self.pair_headroom = 1.25      # pair-buffer capacity factor for resampled steps
         self.save_models = False       # write model pickles at model_save_freq
         for key in kwargs:

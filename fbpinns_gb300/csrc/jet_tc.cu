@@ -1,0 +1,61 @@
+// C ABI of the tensor-core forward jet kernel (tcgen05, 3xTF32) for networks
+// with two 16-wide hidden layers.
+#include <algorithm>
+
+#include "jet_tc.cuh"
+
+namespace fbp {
+
+template <int XD, int D2>
+static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs& pr, float* pair_out,
+                             int32_t* status, int grid, cudaStream_t st) {
+    using C = Cfg<XD, 16, 16, D2>;
+    FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward_tc: nparam %d != %d for this shape", net.nparam, C::P);
+    const size_t shm = sizeof(TcSmem<C>);
+    static int res = 0;
+    if (!res) {
+        FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)shm));
+        // CTAs that fit on one SM by shared memory, registers and threads: an
+        // upper bound on how many can be resident at once
+        cudaFuncAttributes fa;
+        FBP_CUDA_CHECK(cudaFuncGetAttributes(&fa, forward_pairs_tc_kernel<C>));
+        int dev = 0, smem_sm = 0, regs_sm = 0, thr_sm = 0;
+        FBP_CUDA_CHECK(cudaGetDevice(&dev));
+        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+        const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the driver's 1 KiB per CTA
+        const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
+        res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
+        FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");
+    }
+    // every resident CTA holds COLS of the SM's 512 TMEM columns; more
+    // resident CTAs than that would block in tcgen05.alloc
+    constexpr int cols = TcSmem<C>::COLS;
+    FBP_REQUIRE(res * cols <= 512, FBP_ERR_UNSUPPORTED, "forward_tc: %d CTAs/SM x %d TMEM columns > 512", res, cols);
+    if (grid <= 0) grid = res * sm_count();
+    forward_pairs_tc_kernel<C><<<grid, TC_TILE, shm, st>>>(net, x, pr, pair_out, status);
+    FBP_LAUNCH_CHECK();
+    return FBP_OK;
+}
+
+}  // namespace fbp
+
+extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pairs, float* pair_out,
+                                    int32_t* status, int32_t grid, void* stream) {
+    FBP_REQUIRE(net && pairs && x && pair_out && status, FBP_ERR_INVALID, "fbp_forward_pairs_tc: null argument");
+    FBP_REQUIRE(net->theta && net->xmins && net->xmaxs && net->flags && net->unnorms, FBP_ERR_INVALID,
+                "fbp_forward_pairs_tc: null network pointer");
+    FBP_REQUIRE(pairs->sd_point && pairs->sd_pair && pairs->items && pairs->n_items, FBP_ERR_INVALID,
+                "fbp_forward_pairs_tc: null pair pointer");
+    FBP_REQUIRE(net->ud == 1 && net->h1 == 16 && net->h2 == 16, FBP_ERR_UNSUPPORTED,
+                "fbp_forward_pairs_tc: only the xd-16-16-1 networks are compiled (got h1=%d h2=%d ud=%d)", net->h1,
+                net->h2, net->ud);
+    cudaStream_t st = fbp::as_stream(stream);
+    if (net->xd == 2 && net->d2mask == 3) return fbp::launch_forward_tc<2, 3>(*net, x, *pairs, pair_out, status, grid, st);
+    if (net->xd == 2 && net->d2mask == 1) return fbp::launch_forward_tc<2, 1>(*net, x, *pairs, pair_out, status, grid, st);
+    if (net->xd == 2 && net->d2mask == 0) return fbp::launch_forward_tc<2, 0>(*net, x, *pairs, pair_out, status, grid, st);
+    fbp::set_error("fbp_forward_pairs_tc: no compiled kernel for xd=%d d2mask=%d", net->xd, net->d2mask);
+    return FBP_ERR_UNSUPPORTED;
+}

@@ -1,0 +1,319 @@
+// Tensor-core (tcgen05, 3xTF32) variant of the per-pair forward jet kernel for
+// networks with two 16-wide hidden layers.
+//
+// Layer 2 of the jet, z_c[k] = sum_n W2[k][n] v_c[n] (+ b2[k] for c = 0), is
+// J small GEMMs per tile of 128 pairs (M = 128 pairs, N = 16, K = 16).  The
+// layer-1 jet components factor as v_0 = a, v_{1+d} = tp * cw[:, d] and
+// v_{1+xd+s} = tpp * cw2[:, d_s] (tp = 1 - a^2, tpp = -2 a tp, cw = W1 / sd),
+// so the pair-dependent A operands are only a, tp and tpp, and the per-neuron
+// scale moves into B: B_c = W2 diag(f_c), f_c = 1, cw[:, d] or cw2[:, d_s],
+// built once per work item.  Each thread writes its pair's rows of a, tp, tpp
+// into shared memory, split as v = hi + lo with hi = v truncated to TF32, in
+// the no-swizzle K-major layout of 8-row x 16-byte core matrices; one thread
+// issues hi*hi + hi*lo + lo*hi MMAs (3xTF32, FP32 accumulation) into TMEM
+// columns [16c, 16c+16); every thread reads back its own TMEM lane (= its
+// pair) with tcgen05.ld.  The rest of the jet (tanh rules, output layer,
+// unnormalisation, window) stays on the CUDA cores as in forward_pairs_kernel.
+//
+// Waits on the MMA-completion mbarrier are bounded: on a time-out the kernel
+// records FBP_STATUS_TC_TIMEOUT in the status word, stops issuing work, waits
+// once more (bounded) and frees its TMEM before returning.
+#pragma once
+
+#include "jet.cuh"
+
+namespace fbp {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets between core matrices, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t umma_idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: true when the phase completed, false once limit_ns of wall
+// time has passed without it.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(mbar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Byte offset of element (row, k) of a K-major operand with 16 K-elements per
+// row in the no-swizzle core-matrix layout: core matrix (row/8, k/4) at
+// (row/8)*512 + (k/4)*128, 16 bytes per row inside it.
+__device__ __forceinline__ uint32_t kmajor16_off(int row, int k) {
+    return (uint32_t)((row >> 3) * 512 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
+    hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+    lo = v - hi;
+}
+
+constexpr int TC_TILE = 128;   // pairs per tile = MMA M = threads per CTA = TMEM lanes
+constexpr uint64_t TC_WAIT_NS = 200000000ull;  // 0.2 s: an MMA group takes microseconds
+
+template <class C>
+struct TcSmem {
+    static_assert(C::TWO && C::H1 == 16 && C::H2 == 16 && C::J <= 8, "tensor-core shape");
+    // TMEM columns allocated per CTA: J accumulators of 16 columns, rounded up
+    // to the power of two >= 32 that tcgen05.alloc takes
+    static constexpr int COLS = pow2_at_least(C::J * 16 < 32 ? 32 : C::J * 16);
+    static constexpr int NA = C::NS > 0 ? 3 : 2;  // A operands: a, tp (, tpp)
+    // A operands, hi and lo, each 128 rows x 16 TF32 = 8 KiB
+    float a[NA][2][TC_TILE * 16];
+    // B operands per jet component (16 x 16): hi, lo
+    float b[C::J][2][16 * 16];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+// A operand of jet component c: 0 = a, 1 = tp, 2 = tpp.
+template <class C>
+__host__ __device__ constexpr int tc_a_of(int c) {
+    return c == 0 ? 0 : (c <= C::XD ? 1 : 2);
+}
+
+template <class C>
+__global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, const float* __restrict__ x,
+                                                                    fbp_pairs pr, float* __restrict__ pair_out,
+                                                                    int32_t* __restrict__ status) {
+    constexpr int J = C::J, XD = C::XD, RS = rec_stride(C::J), H1 = 16, H2 = 16;
+    constexpr int NA = TcSmem<C>::NA;
+    __shared__ SParams<C> S;
+    extern __shared__ float4 dyn_smem[];
+    TcSmem<C>& T = *reinterpret_cast<TcSmem<C>*>(dyn_smem);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t mbar = smem_u32(&T.mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&T.tmem_base)),
+                     "r"(TcSmem<C>::COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = T.tmem_base;
+    constexpr uint32_t idesc = umma_idesc_tf32(TC_TILE, H2);
+    uint32_t phase = 0;
+    bool failed = false;
+    const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
+    for (int it = blockIdx.x; it < nit && !failed; it += gridDim.x) {
+        const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
+        __syncthreads();
+        load_params<C>(S, net, j);
+        // B_c[k][n] = W2[k][n] f_c[n], split hi/lo, rows k, K = n
+        for (int i = tid; i < J * H2 * H1; i += blockDim.x) {
+            const int c = i / (H2 * H1), r = i - c * (H2 * H1);
+            const int k = r / H1, n = r - k * H1;
+            float f = 1.0f;
+            if (c >= 1 && c <= XD) f = S.cw[n * XD + (c - 1)];
+            if (c > XD) f = S.cw2[n * XD + C::sd_dim(c - 1 - XD)];
+            float hi, lo;
+            split_tf32(S.W2[r] * f, hi, lo);
+            const uint32_t off = kmajor16_off(k, n) >> 2;
+            T.b[c][0][off] = hi;
+            T.b[c][1][off] = lo;
+        }
+        // the first tile's pair (prefetched; later tiles are prefetched while
+        // the previous tile's MMAs run)
+        int pos_n = 0;
+        float xr_n[XD];
+#pragma unroll
+        for (int d = 0; d < XD; ++d) xr_n[d] = 0.f;
+        if (tid < cnt) {
+            const int pt = pr.sd_point[beg + tid];
+            pos_n = pr.sd_pair[beg + tid];
+#pragma unroll
+            for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+        }
+        for (int t0 = 0; t0 < cnt; t0 += TC_TILE) {
+            const bool act = t0 + tid < cnt;
+            const int pos = pos_n;
+            float xn[XD];
+#pragma unroll
+            for (int d = 0; d < XD; ++d) xn[d] = (xr_n[d] - S.mu[d]) * S.inv_sd[d];
+            // this pair's rows of the A operands
+#pragma unroll
+            for (int n4 = 0; n4 < H1; n4 += 4) {
+                float av[NA][4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float a = l1_act<C>(S, xn, n4 + q);
+                    const float tp = 1.0f - a * a;
+                    av[0][q] = a;
+                    av[1][q] = tp;
+                    if constexpr (NA > 2) av[NA - 1][q] = -2.0f * a * tp;
+                }
+                const uint32_t off = kmajor16_off(tid, n4) >> 2;
+#pragma unroll
+                for (int o = 0; o < NA; ++o) {
+                    float h[4], l[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) split_tf32(av[o][q], h[q], l[q]);
+                    *reinterpret_cast<float4*>(&T.a[o][0][off]) = make_float4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<float4*>(&T.a[o][1][off]) = make_float4(l[0], l[1], l[2], l[3]);
+                }
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+#pragma unroll
+                for (int c = 0; c < J; ++c) {
+                    const int o = tc_a_of<C>(c);
+                    const uint32_t ah = smem_u32(&T.a[o][0][0]), al = smem_u32(&T.a[o][1][0]);
+                    const uint32_t bh = smem_u32(&T.b[c][0][0]), bl = smem_u32(&T.b[c][1][0]);
+                    const uint32_t d = tmem + (uint32_t)(c * 16);
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        const uint32_t ko = ks * 256;  // two 16-byte K chunks per MMA (K = 8)
+                        umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, ks > 0);
+                        umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bl + ko, 128, 512), idesc, 1);
+                        umma_tf32(d, umma_desc(al + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, 1);
+                    }
+                }
+                umma_commit(mbar);
+            }
+            // prefetch the next tile's pair while the MMAs run
+            const int tn = t0 + TC_TILE + tid;
+            if (tn < cnt) {
+                const int pt = pr.sd_point[beg + tn];
+                pos_n = pr.sd_pair[beg + tn];
+#pragma unroll
+                for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+            }
+            float w[J];
+            window_jet<C>(S, xn, w);
+            // every thread waits; the verdict is made CTA-uniform before the
+            // warp-collective tcgen05.ld below
+            failed = __syncthreads_or(!mbar_wait_bounded(mbar, phase, TC_WAIT_NS));
+            if (failed) {
+                if (tid == 0) atomicOr(status, FBP_STATUS_TC_TIMEOUT);
+                break;
+            }
+            phase ^= 1u;
+            tc_fence_after();
+            float acc[J][16];
+#pragma unroll
+            for (int c = 0; c < J; ++c) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), acc[c]);
+            tmem_wait_ld();
+            if (act) {
+                float o[J];
+#pragma unroll
+                for (int c = 0; c < J; ++c) o[c] = 0.f;
+                o[0] = S.b3;
+#pragma unroll
+                for (int k = 0; k < H2; ++k) {
+                    float z[J], g[J], a, tp, tpp;
+#pragma unroll
+                    for (int c = 0; c < J; ++c) z[c] = acc[c][k];
+                    z[0] += S.b2[k];
+                    tanh_jet<C>(z, g, a, tp, tpp);
+                    const float w3 = S.W3[k];
+#pragma unroll
+                    for (int c = 0; c < J; ++c) o[c] = fmaf(w3, g[c], o[c]);
+                }
+                float u[J];
+#pragma unroll
+                for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
+                u[0] += S.mu_u;
+                float rec[RS];
+                rec[0] = u[0] * w[0];
+#pragma unroll
+                for (int d = 0; d < XD; ++d) rec[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
+#pragma unroll
+                for (int s = 0; s < C::NS; ++s) {
+                    const int d = C::sd_dim(s);
+                    rec[1 + XD + s] = u[1 + XD + s] * w[0] + 2.0f * u[1 + d] * w[1 + d] + u[0] * w[1 + XD + s];
+                }
+#pragma unroll
+                for (int c = 0; c < J; ++c) rec[J + c] = w[c];
+#pragma unroll
+                for (int c = 2 * J; c < RS; ++c) rec[c] = 0.f;
+                float4* dst = reinterpret_cast<float4*>(pair_out + (size_t)pos * RS);
+#pragma unroll
+                for (int q = 0; q < RS / 4; ++q)
+                    dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
+            }
+            tc_fence_before();
+            __syncthreads();  // TMEM and the A rows are reused by the next tile
+            tc_fence_after();
+        }
+    }
+    if (failed) mbar_wait_bounded(mbar, phase, TC_WAIT_NS);  // let the timed-out MMAs finish
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TcSmem<C>::COLS) : "memory");
+}
+
+}  // namespace fbp

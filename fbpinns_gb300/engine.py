@@ -194,10 +194,15 @@ def t_status(ps):
     return ps.takes.status
 
 
+def tc_supported(xd, h1, h2):
+    """True where the tensor-core forward kernel is compiled (xd = 2, two 16-wide hidden layers)."""
+    return xd == 2 and h1 == 16 and h2 == 16
+
+
 class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
-    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None):
+    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None, tensor_cores=None):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -223,6 +228,12 @@ class FBPINNEngine:
         self.J = jet_size(self.xd, self.d2mask)
         self.chunk = int(chunk)
         self.launch_grid = int(grid) if grid else 0
+        # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
+        # None = wherever available, True = required, False = CUDA-core FMA kernel
+        tc_ok = tc_supported(self.xd, self.h1, self.h2)
+        if tensor_cores and not tc_ok:
+            raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} (compiled: 2-16-16-1)")
+        self.tensor_cores = tc_ok if tensor_cores is None else bool(tensor_cores)
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
         self.m1 = torch.zeros_like(self.theta)
@@ -282,6 +293,11 @@ class FBPINNEngine:
         lib = _lib.load()
         net = self.net_struct(theta)
         pr = ps.pairs_struct(False)
+        if self.tensor_cores:
+            _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
+                                                _lib.ptr(ps.takes.status), 0, _lib.stream_ptr(stream)),
+                       "fbp_forward_pairs_tc")
+            return
         _lib.check(lib.fbp_forward_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
                                          self.launch_grid, _lib.stream_ptr(stream)), "fbp_forward_pairs")
 

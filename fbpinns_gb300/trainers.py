@@ -261,7 +261,8 @@ class FBPINNTrainer:
         required = [con[-1] for con in constraints_global]
         constraints_global = [con[:-1] for con in constraints_global]
         d2 = d2mask_of(required, xd)
-        eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid)
+        eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
+                           tensor_cores=getattr(c, "tensor_cores", None))
         eng.set_theta(pack_layers(net_tr["layers"]))
         for k, v in list(all_params["trainable"].get("problem", {}).items()):
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()

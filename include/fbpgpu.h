@@ -54,6 +54,7 @@ extern "C" {
 #define FBP_STATUS_ITEM_OVERFLOW 4      /* more work items than capacity */
 #define FBP_STATUS_LEVEL_ORDER 8        /* a point's levels are not in ascending model order */
 #define FBP_STATUS_BAD_INDEX 16         /* an index out of range was skipped */
+#define FBP_STATUS_TC_TIMEOUT 32        /* a tensor-core kernel gave up waiting for its MMAs */
 
 /* Maximum compiled sizes. */
 #define FBP_MAX_XD 3
@@ -224,6 +225,16 @@ int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t* select, in
  * decompositions.py:184-199; windows.py:25-35). */
 int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs,
                       float* pair_out, int32_t grid, void* stream);
+
+/* Same records as fbp_forward_pairs, with layer 2 of every jet component on
+ * the 5th-generation tensor cores (tcgen05, TF32 operands split hi + lo, three
+ * products, FP32 accumulation in tensor memory).  Compiled for xd = 2 with two
+ * 16-wide hidden layers only (FBP_ERR_UNSUPPORTED otherwise).  A kernel that
+ * times out waiting for its MMAs sets FBP_STATUS_TC_TIMEOUT in *status and
+ * leaves its remaining pairs unwritten.  Same reference functions as
+ * fbp_forward_pairs. */
+int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pairs,
+                         float* pair_out, int32_t* status, int32_t grid, void* stream);
 
 /* 1 if the per-pair jet kernels are compiled for this network shape and jet
  * mask (ud = 1), else 0.  Lets a caller fail early with a clear message. */

@@ -1,0 +1,81 @@
+"""Tensor-core (tcgen05, 3xTF32) forward jets vs the CUDA-core FMA kernel.
+
+Both kernels write the same per-pair records (jets of u*w and of w); the
+tensor-core one computes layer 2 with TF32 operands split hi + lo and three
+products, so it agrees with the FP32 FMA path to FP32 rounding, not bitwise.
+Tolerance: max |difference| per jet component below 2e-5 of that component's
+largest magnitude.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import decomposition, random_layers, layer_sizes
+from fbpinns_gb300 import _lib
+from fbpinns_gb300.engine import FBPINNEngine
+from fbpinns_gb300.networks import pack_layers
+
+pytestmark = pytest.mark.gpu
+
+TC_TOL = 2e-5
+
+
+def _records(recipe, d2, n, seed, chunk=512):
+    static = decomposition(recipe)
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = random_layers([2, 16, 16, 1], m, seed)
+    eng = FBPINNEngine(static, layer_sizes(layers), d2, chunk=chunk, tensor_cores=False)
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    g = torch.Generator().manual_seed(seed)
+    ps = eng.points(torch.rand((n, 2), generator=g))
+    lib = _lib.load()
+    net, pr = eng.net_struct(None), ps.pairs_struct(False)
+    eng.forward_pairs(ps)
+    ref = ps.pair_out[:ps.s].clone()
+    ps.pair_out.fill_(float("nan"))
+    status = torch.zeros(1, dtype=torch.int32, device=ps.x.device)
+    _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
+                                        _lib.ptr(status), 0, _lib.stream_ptr()), "fbp_forward_pairs_tc")
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0, _lib.decode_status(int(status.item()))
+    return ref, ps.pair_out[:ps.s].clone(), eng.J
+
+
+def _check(ref, tc, J):
+    assert torch.isfinite(tc).all()
+    for c in range(2 * J):
+        scale = ref[:, c].abs().max().item()
+        err = (tc[:, c] - ref[:, c]).abs().max().item()
+        assert err <= TC_TOL * max(scale, 1e-30), (c, err, scale)
+
+
+@pytest.mark.parametrize("d2", [3, 1, 0])
+def test_tensor_core_forward_matches_fma_small(cuda, d2):
+    """Four-level decomposition (85 subdomains), 3000 points, all three jet masks."""
+    ref, tc, J = _records("multilevel", d2, 3000, seed=5 + d2)
+    _check(ref, tc, J)
+
+
+def test_tensor_core_forward_matches_fma_poisson(cuda):
+    """Six-level Poisson decomposition (1365 subdomains), 2^16 points: many
+    full and partial 128-pair tiles per work item."""
+    ref, tc, J = _records("poisson", 3, 1 << 16, seed=11)
+    _check(ref, tc, J)
+
+
+def test_tensor_core_forward_rejects_other_shapes(cuda):
+    static = decomposition("multilevel")
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = random_layers([2, 8, 8, 1], m, 1)
+    eng = FBPINNEngine(static, layer_sizes(layers), 3)
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    ps = eng.points(torch.rand((100, 2)))
+    lib = _lib.load()
+    status = torch.zeros(1, dtype=torch.int32, device=ps.x.device)
+    rc = lib.fbp_forward_pairs_tc(C.byref(eng.net_struct(None)), _lib.ptr(ps.x), C.byref(ps.pairs_struct(False)),
+                                  _lib.ptr(ps.pair_out), _lib.ptr(status), 0, _lib.stream_ptr())
+    assert rc == -3  # FBP_ERR_UNSUPPORTED
+    assert b"16-16" in lib.fbp_last_error()
