@@ -42,7 +42,7 @@ class Net(C.Structure):
 
 
 class Pairs(C.Structure):
-    _fields_ = [("sd_start", C.c_void_p), ("sd_pair", C.c_void_p), ("sd_point", C.c_void_p), ("sd_slot", C.c_void_p),
+    _fields_ = [("sd_start", C.c_void_p), ("sd_rec", C.c_void_p),
                 ("items", C.c_void_p), ("n_items", C.c_void_p), ("items_cap", C.c_int64), ("slots_cap", C.c_int64)]
 
 
@@ -66,7 +66,7 @@ _SIG = {
     "fbp_compact_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_compact_flags": (C.c_int, [_P, _I64, _P, _P, _P, C.c_size_t, _P]),
     "fbp_sort_scratch_bytes": (C.c_size_t, [_I64, _I64]),
-    "fbp_sort_pairs": (C.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _P, _P, _P, _P, C.c_size_t, _P]),
+    "fbp_sort_pairs": (C.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _P, _P, C.c_size_t, _P]),
     "fbp_work_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_build_work": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, C.c_size_t, _P]),
     "fbp_forward_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _I32, _P]),

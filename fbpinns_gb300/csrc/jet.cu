@@ -10,7 +10,7 @@ static int check_net(const fbp_net* net, const fbp_pairs* pr) {
     FBP_REQUIRE(net && pr, FBP_ERR_INVALID, "jet: null descriptor");
     FBP_REQUIRE(net->theta && net->xmins && net->xmaxs && net->flags && net->unnorms, FBP_ERR_INVALID,
                 "jet: null network pointer");
-    FBP_REQUIRE(pr->sd_point && pr->sd_pair && pr->sd_slot && pr->items && pr->n_items, FBP_ERR_INVALID,
+    FBP_REQUIRE(pr->sd_rec && pr->items && pr->n_items, FBP_ERR_INVALID,
                 "jet: null pair pointer");
     FBP_REQUIRE(net->ud == 1, FBP_ERR_UNSUPPORTED, "jet: ud=%d (only scalar outputs are compiled)", net->ud);
     return FBP_OK;

@@ -37,6 +37,11 @@ struct Cfg {
     __host__ __device__ static constexpr int sd_dim(int s) { return DimsOf<D2>::get(s); }
 };
 
+// the sorted pair record (point-major pair index, point, slot, 0)
+__device__ __forceinline__ int4 pair_rec(const fbp_pairs& pr, int64_t e) {
+    return __ldg(reinterpret_cast<const int4*>(pr.sd_rec) + e);
+}
+
 template <class C>
 struct SParams {
     float W1[C::H1 * C::XD];
@@ -278,8 +283,9 @@ __global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net n
 #pragma unroll
         for (int d = 0; d < XD; ++d) xr_n[d] = 0.f;
         if (t < cnt) {
-            const int pt = pr.sd_point[beg + t];
-            pos_n = pr.sd_pair[beg + t];
+            const int4 r = pair_rec(pr, beg + t);
+            const int pt = r.y;
+            pos_n = r.x;
 #pragma unroll
             for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
         }
@@ -290,8 +296,9 @@ __global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net n
             for (int d = 0; d < XD; ++d) xn[d] = (xr_n[d] - S.mu[d]) * S.inv_sd[d];
             const int tn = t + blockDim.x;
             if (tn < cnt) {
-                const int pt = pr.sd_point[beg + tn];
-                pos_n = pr.sd_pair[beg + tn];
+                const int4 r = pair_rec(pr, beg + tn);
+                const int pt = r.y;
+                pos_n = r.x;
 #pragma unroll
                 for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
             }
@@ -427,8 +434,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             float* a1row = &R.a1[lane * A::AS];
             if (act) {
                 const int e = beg + t0 + lane;
-                const int pt = pr.sd_point[e];
-                const int slot = pr.sd_slot[e];
+                const int4 r = pair_rec(pr, e);
+                const int pt = r.y;
+                const int slot = r.z;
                 load_point<C>(S, x, pt, xn);
                 float w[J];
                 window_jet<C>(S, xn, w);

@@ -47,7 +47,7 @@ extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fb
     FBP_REQUIRE(net && pairs && x && pair_out && status, FBP_ERR_INVALID, "fbp_forward_pairs_tc: null argument");
     FBP_REQUIRE(net->theta && net->xmins && net->xmaxs && net->flags && net->unnorms, FBP_ERR_INVALID,
                 "fbp_forward_pairs_tc: null network pointer");
-    FBP_REQUIRE(pairs->sd_point && pairs->sd_pair && pairs->items && pairs->n_items, FBP_ERR_INVALID,
+    FBP_REQUIRE(pairs->sd_rec && pairs->items && pairs->n_items, FBP_ERR_INVALID,
                 "fbp_forward_pairs_tc: null pair pointer");
     FBP_REQUIRE(net->ud == 1 && net->h1 == 16 && net->h2 == 16, FBP_ERR_UNSUPPORTED,
                 "fbp_forward_pairs_tc: only the xd-16-16-1 networks are compiled (got h1=%d h2=%d ud=%d)", net->h1,

@@ -188,8 +188,9 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
 #pragma unroll
         for (int d = 0; d < XD; ++d) xr_n[d] = 0.f;
         if (tid < cnt) {
-            const int pt = pr.sd_point[beg + tid];
-            pos_n = pr.sd_pair[beg + tid];
+            const int4 r = pair_rec(pr, beg + tid);
+            const int pt = r.y;
+            pos_n = r.x;
 #pragma unroll
             for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
         }
@@ -245,8 +246,9 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             // prefetch the next tile's pair while the MMAs run
             const int tn = t0 + TC_TILE + tid;
             if (tn < cnt) {
-                const int pt = pr.sd_point[beg + tn];
-                pos_n = pr.sd_pair[beg + tn];
+                const int4 r = pair_rec(pr, beg + tn);
+                const int pt = r.y;
+                pos_n = r.x;
 #pragma unroll
                 for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
             }

@@ -68,62 +68,104 @@ __global__ void inside_count_kernel(const float* __restrict__ x, int64_t n, fbp_
     }
 }
 
-// One warp per point: the lanes test 32 consecutive candidates of the point's
-// cell at a time (candidates ascend by box id) and write the hits at
-// ballot-ranked consecutive positions, so each point's pairs are written
-// coalesced and in ascending box order.
+// Fill: one thread per point tests the candidates of its cell (the box arrays
+// are small and stay in L1); a warp's 32 consecutive points own one contiguous
+// range of the point-major pair arrays, so their hits are staged in shared
+// memory and the warp writes the range out coalesced.  A warp whose range
+// exceeds its staging space writes its points' pairs directly.  A staged pair
+// is one int32: box id << 11 | POU level << 5 | point within the warp
+// (box ids below 2^21, checked by the caller).
+constexpr int FILL_WARPS = 8;     // warps per CTA
+constexpr int FILL_STAGE = 1280;  // staged pairs per warp
+constexpr int64_t FILL_MAX_M = int64_t(1) << 21;
+
 template <int XD>
-__global__ void inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b,
-                                   const int32_t* __restrict__ pt_off, const int32_t* __restrict__ np_off,
-                                   const uint64_t* __restrict__ pt_lvl, int32_t* __restrict__ n_take,
-                                   int32_t* __restrict__ m_take, int32_t* __restrict__ p_take,
-                                   int32_t* __restrict__ np_take, int64_t s_cap, int64_t u_cap,
-                                   int32_t* __restrict__ status) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t p = warp; p < n; p += nwarps) {
-        float xp[XD];
+__global__ void __launch_bounds__(FILL_WARPS * 32)
+    inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b, const int32_t* __restrict__ pt_off,
+                       const int32_t* __restrict__ np_off, const uint64_t* __restrict__ pt_lvl,
+                       int32_t* __restrict__ n_take, int32_t* __restrict__ m_take, int32_t* __restrict__ p_take,
+                       int32_t* __restrict__ np_take, int64_t s_cap, int64_t u_cap, int32_t* __restrict__ status) {
+    __shared__ int32_t stage[FILL_WARPS][FILL_STAGE];
+    __shared__ uint64_t s_lvl[FILL_WARPS][32];
+    __shared__ int32_t s_ubase[FILL_WARPS][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * FILL_WARPS;
+    for (int64_t p0 = ((int64_t)blockIdx.x * FILL_WARPS + w) * 32; p0 < n; p0 += nwarps * 32) {
+        const int64_t p = p0 + lane;
+        const bool valid = p < n;
+        const int np = (int)min((int64_t)32, n - p0);
+        const int64_t wb = pt_off[p0], we = pt_off[p0 + np];
+        const int64_t total = we - wb;
+        const bool staged = total <= FILL_STAGE && b.m <= FILL_MAX_M;
+        int64_t base = 0;
+        int32_t ubase = 0;
+        uint64_t lvl = 0;
+        if (valid) {
+            base = pt_off[p];
+            ubase = np_off[p];
+            lvl = pt_lvl[p];
+        }
+        s_lvl[w][lane] = lvl;
+        s_ubase[w][lane] = ubase;
+        if (valid) {
+            float xp[XD];
 #pragma unroll
-        for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
-        const int c = cell_of<XD>(xp, b);
-        const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
-        const uint64_t lvl = pt_lvl[p];
-        const int64_t base = pt_off[p];
-        const int64_t ubase = np_off[p];
-        int64_t k = 0;
-        for (int e = e0; e < e1; e += 32) {
-            const int ee = e + lane;
-            int j = -1;
-            bool hit = false;
-            if (ee < e1) {
-                j = b.cell_boxes[ee];
-                hit = (!b.select || b.select[j]) && inside_box<XD>(xp, b.xmins, b.xmaxs, j);
+            for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
+            const int c = cell_of<XD>(xp, b);
+            const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
+            int64_t k = 0;
+            for (int e = e0; e < e1; ++e) {
+                const int j = b.cell_boxes[e];
+                if (b.select && !b.select[j]) continue;
+                if (!inside_box<XD>(xp, b.xmins, b.xmaxs, j)) continue;
+                const int lv = b.pou[j] & 63;
+                const int64_t q = base + k - wb;
+                if (staged) {
+                    if (q >= 0 && q < total)
+                        stage[w][q] = (int32_t)(((uint32_t)j << 11) | (uint32_t)(lv << 5) | (uint32_t)lane);
+                    else
+                        atomicOr(status, FBP_STATUS_BAD_INDEX);
+                } else {
+                    const int64_t o = base + k;
+                    if (o < s_cap) {
+                        const uint64_t below = lv ? (lvl & ((1ull << lv) - 1ull)) : 0ull;
+                        n_take[o] = (int32_t)p;
+                        m_take[o] = j;
+                        p_take[o] = ubase + __popcll(below);
+                    } else {
+                        atomicOr(status, FBP_STATUS_PAIR_OVERFLOW);
+                    }
+                }
+                ++k;
             }
-            const unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (hit) {
-                const int64_t o = base + k + __popc(m & ((1u << lane) - 1u));
+            // unique (point, level) slots in ascending level order
+            const int nl = __popcll(lvl);
+            for (int r = 0; r < nl; ++r) {
+                const int64_t o = (int64_t)ubase + r;
+                if (o < u_cap)
+                    np_take[o] = (int32_t)p;
+                else
+                    atomicOr(status, FBP_STATUS_SLOT_OVERFLOW);
+            }
+        }
+        __syncwarp();
+        if (staged) {
+            for (int64_t q = lane; q < total; q += 32) {
+                const int32_t v = stage[w][q];
+                const int idx = v & 31, lv = (v >> 5) & 63;
+                const int64_t o = wb + q;
                 if (o < s_cap) {
-                    const int lv = b.pou[j] & 63;
-                    const uint64_t below = lv ? (lvl & ((1ull << lv) - 1ull)) : 0ull;
-                    n_take[o] = (int32_t)p;
-                    m_take[o] = j;
-                    p_take[o] = (int32_t)(ubase + __popcll(below));
+                    const uint64_t l = s_lvl[w][idx];
+                    const uint64_t below = lv ? (l & ((1ull << lv) - 1ull)) : 0ull;
+                    n_take[o] = (int32_t)(p0 + idx);
+                    m_take[o] = (int32_t)((uint32_t)v >> 11);
+                    p_take[o] = s_ubase[w][idx] + __popcll(below);
                 } else {
                     atomicOr(status, FBP_STATUS_PAIR_OVERFLOW);
                 }
             }
-            k += __popc(m);
         }
-        // unique (point, level) slots in ascending level order: lane r writes slots r, r+32
-        const int nl = __popcll(lvl);
-        for (int r = lane; r < nl; r += 32) {
-            const int64_t o = ubase + r;
-            if (o < u_cap)
-                np_take[o] = (int32_t)p;
-            else
-                atomicOr(status, FBP_STATUS_SLOT_OVERFLOW);
-        }
+        __syncwarp();
     }
 }
 
@@ -292,11 +334,17 @@ __global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t*
     }
 }
 
+constexpr int SCATTER_U = 4;  // 32-pair rows whose loads are issued together
+
+// One warp per chunk of SORT_CH pairs (point-major).  A point's pairs have
+// distinct boxes, so each row of 32 pairs is placed point by point: the lanes
+// of one point read and advance distinct bucket counters, and the points of
+// the row follow each other in order -- a stable counting sort with no
+// intra-warp key matching.
 __global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
                                     const int32_t* __restrict__ p_take, const int32_t* __restrict__ s_dev,
                                     int64_t s_cap, int64_t m, int64_t nchunks,
-                                    const int32_t* __restrict__ hoff, int32_t* __restrict__ sd_pair,
-                                    int32_t* __restrict__ sd_point, int32_t* __restrict__ sd_slot) {
+                                    const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
     extern __shared__ int run[];  // per-bucket running offsets of this chunk
     const int lane = threadIdx.x;  // blockDim.x == 32
     const int64_t s = min((int64_t)*s_dev, s_cap);
@@ -304,25 +352,39 @@ __global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32
         for (int64_t j = lane; j < m; j += 32) run[j] = hoff[j * nchunks + ch];
         __syncwarp();
         const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
-        for (int64_t i0 = b0; i0 < b1; i0 += 32) {
-            const int64_t i = i0 + lane;
-            const bool valid = i < b1;
-            int k = valid ? key[i] : -1;
-            if (valid && (k < 0 || k >= m)) k = -1;
-            const unsigned act = __ballot_sync(0xffffffffu, k >= 0);
-            const unsigned peers = __match_any_sync(0xffffffffu, k);
-            if (k >= 0) {
-                const unsigned lt = peers & ((1u << lane) - 1u);
-                const int leader = __ffs(peers) - 1;
-                const int base = run[k];
-                const int o = base + __popc(lt);
-                sd_pair[o] = (int32_t)i;
-                sd_point[o] = n_take[i];
-                sd_slot[o] = p_take[i];
-                __syncwarp(act);
-                if (lane == leader) run[k] = base + __popc(peers);
+        for (int64_t i0 = b0; i0 < b1; i0 += 32 * SCATTER_U) {
+            int kk[SCATTER_U], nn[SCATTER_U], pp[SCATTER_U];
+#pragma unroll
+            for (int u = 0; u < SCATTER_U; ++u) {
+                const int64_t i = i0 + u * 32 + lane;
+                kk[u] = -1;
+                nn[u] = -1;
+                pp[u] = 0;
+                if (i < b1) {
+                    kk[u] = key[i];
+                    nn[u] = n_take[i];
+                    pp[u] = p_take[i];
+                }
             }
-            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < SCATTER_U; ++u) {
+                const int64_t i = i0 + u * 32 + lane;
+                const int k = kk[u];
+                const bool ok = k >= 0 && k < m;
+                unsigned todo = __ballot_sync(0xffffffffu, i < b1);
+                while (todo) {
+                    // the row's next point: the lanes holding it form one group
+                    const int pt = __shfl_sync(0xffffffffu, nn[u], __ffs(todo) - 1);
+                    const unsigned grp = __ballot_sync(0xffffffffu, (todo >> lane & 1u) && nn[u] == pt);
+                    if ((grp >> lane & 1u) && ok) {
+                        const int o = run[k];
+                        run[k] = o + 1;
+                        sd_rec[o] = make_int4((int32_t)i, pt, pp[u], 0);
+                    }
+                    todo &= ~grp;
+                    __syncwarp();
+                }
+            }
         }
         __syncwarp();
     }
@@ -434,12 +496,12 @@ extern "C" int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes
     FBP_REQUIRE((n_take && m_take && p_take) || s_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null take");
     FBP_REQUIRE(np_take || u_cap == 0, FBP_ERR_INVALID, "fbp_inside_fill: null np_take");
     if (n == 0) return FBP_OK;
-    const int g = grid_for(n * 32, 256, 8);  // one warp per point
+    const int g = grid_for(n, FILL_WARPS * 32, 8);  // 32 points per warp
     cudaStream_t st = as_stream(stream);
     switch (boxes->xd) {
-        case 1: inside_fill_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
-        case 2: inside_fill_kernel<2><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
-        case 3: inside_fill_kernel<3><<<g, 256, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 1: inside_fill_kernel<1><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 2: inside_fill_kernel<2><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 3: inside_fill_kernel<3><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
     }
     FBP_LAUNCH_CHECK();
     return FBP_OK;
@@ -487,11 +549,12 @@ extern "C" size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m) {
 }
 
 extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
-                              const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_pair,
-                              int32_t* sd_point, int32_t* sd_slot, void* scratch, size_t scratch_bytes,
+                              const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_rec,
+                              void* scratch, size_t scratch_bytes,
                               void* stream) {
     FBP_REQUIRE(s_dev && sd_start && m > 0, FBP_ERR_INVALID, "fbp_sort_pairs: bad args");
-    FBP_REQUIRE(s_cap == 0 || (m_take && n_take && p_take && sd_pair && sd_point && sd_slot), FBP_ERR_INVALID,
+    FBP_REQUIRE(((uintptr_t)sd_rec & 15) == 0, FBP_ERR_INVALID, "fbp_sort_pairs: sd_rec must be 16-byte aligned");
+    FBP_REQUIRE(s_cap == 0 || (m_take && n_take && p_take && sd_rec), FBP_ERR_INVALID,
                 "fbp_sort_pairs: null pointer");
     FBP_REQUIRE(m * 4 <= 200 * 1024, FBP_ERR_UNSUPPORTED, "fbp_sort_pairs: m=%lld exceeds the shared-memory histogram",
                 (long long)m);
@@ -517,8 +580,8 @@ extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, cons
     if (rc) return rc;
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32);
-        sort_scatter_kernel<<<g, 32, shm, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff, sd_pair,
-                                                 sd_point, sd_slot);
+        sort_scatter_kernel<<<g, 32, shm, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff,
+                                                 reinterpret_cast<int4*>(sd_rec));
         FBP_LAUNCH_CHECK();
         sort_starts_kernel<<<grid_for(m + 1, 256), 256, 0, st>>>(hoff, m, nch, sd_start);
         FBP_LAUNCH_CHECK();

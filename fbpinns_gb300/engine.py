@@ -113,9 +113,9 @@ class PointSet:
         self.s_cap, self.u_cap = s_cap, u_cap
         i32 = dict(dtype=torch.int32, device=dev)
         self.sd_start = torch.zeros(m + 1, **i32)
-        self.sd_pair = torch.zeros(max(s_cap, 1), **i32)
-        self.sd_point = torch.zeros(max(s_cap, 1), **i32)
-        self.sd_slot = torch.zeros(max(s_cap, 1), **i32)
+        # sorted pair records (pair, point, slot, 0); the three views below
+        self.sd_rec = torch.zeros((max(s_cap, 1), 4), **i32)
+        self.sd_pair, self.sd_point, self.sd_slot = self.sd_rec[:, 0], self.sd_rec[:, 1], self.sd_rec[:, 2]
         lib = _lib.load()
         self.sort_scratch = torch.empty(int(lib.fbp_sort_scratch_bytes(s_cap, m)) // 4 + 1, **i32)
         self.work_scratch = torch.empty(int(lib.fbp_work_scratch_bytes(m)) // 4 + 1, **i32)
@@ -147,8 +147,7 @@ class PointSet:
         t = self.takes
         _lib.check(lib.fbp_sort_pairs(_lib.ptr(t.m_take), _lib.ptr(t.n_take), _lib.ptr(t.p_take),
                                       _lib.ptr(t.pt_off[self.n:]), self.s_cap, eng.m, _lib.ptr(self.sd_start),
-                                      _lib.ptr(self.sd_pair), _lib.ptr(self.sd_point), _lib.ptr(self.sd_slot),
-                                      _lib.ptr(self.sort_scratch), self.sort_scratch.numel() * 4, st),
+                                      _lib.ptr(self.sd_rec), _lib.ptr(self.sort_scratch), self.sort_scratch.numel() * 4, st),
                    "fbp_sort_pairs")
         self.build_work(stream, state)
 
@@ -171,8 +170,7 @@ class PointSet:
 
     def pairs_struct(self, adjoint=False):
         p = _lib.Pairs()
-        p.sd_start, p.sd_pair = _lib.ptr(self.sd_start), _lib.ptr(self.sd_pair)
-        p.sd_point, p.sd_slot = _lib.ptr(self.sd_point), _lib.ptr(self.sd_slot)
+        p.sd_start, p.sd_rec = _lib.ptr(self.sd_start), _lib.ptr(self.sd_rec)
         if adjoint:
             p.items, p.n_items = _lib.ptr(self.items_act), _lib.ptr(self.n_items_act)
         else:

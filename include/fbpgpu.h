@@ -107,9 +107,9 @@ typedef struct fbp_net {
 /* Pair lists sorted subdomain-major, and the work queue over them. */
 typedef struct fbp_pairs {
     const int32_t* sd_start;  /* (m+1,) offsets of each subdomain's pairs */
-    const int32_t* sd_pair;   /* (s,) point-major pair index of each sorted pair */
-    const int32_t* sd_point;  /* (s,) point index of each sorted pair */
-    const int32_t* sd_slot;   /* (s,) (point, level) slot of each sorted pair */
+    /* (s, 4) one 16-byte record per sorted pair, 16-byte aligned: its
+     * point-major pair index, point index, (point, level) slot, 0 */
+    const int32_t* sd_rec;
     const int32_t* items;     /* (cap, 3) work items: (subdomain, begin, count) */
     const int32_t* n_items;   /* device count of valid items */
     int64_t items_cap;
@@ -199,15 +199,17 @@ int fbp_compact_flags(const int32_t* flag, int64_t n, int32_t* out, int32_t* cou
                       void* scratch, size_t scratch_bytes, void* stream);
 
 /* Stable counting sort of the point-major pairs by subdomain: for each
- * subdomain its pairs in ascending point order.  Writes sd_start (m+1),
- * sd_pair, sd_point, sd_slot.  s_dev is the device pair count (pt_off[n]).
+ * subdomain its pairs in ascending point order.  Writes sd_start (m+1) and
+ * sd_rec (s_cap, 4): per sorted pair its point-major pair index, point,
+ * slot and 0 (sd_rec 16-byte aligned).  The boxes of any one point must be
+ * distinct (as inside_fill writes them).  s_dev is the device pair count
+ * (pt_off[n]).
  * No reference counterpart: the reference gathers per-pair parameter copies
  * (fbpinns/trainers.py:141-145) instead of grouping pairs by subdomain. */
 size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m);
 int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
                    const int32_t* s_dev, int64_t s_cap, int64_t m,
-                   int32_t* sd_start, int32_t* sd_pair, int32_t* sd_point, int32_t* sd_slot,
-                   void* scratch, size_t scratch_bytes, void* stream);
+                   int32_t* sd_start, int32_t* sd_rec, void* scratch, size_t scratch_bytes, void* stream);
 
 /* Work queue: each subdomain with select[j] != 0 (NULL = all) contributes
  * ceil(count/chunk) items (subdomain, begin, count) in subdomain order.
