@@ -60,8 +60,8 @@ _SIG = {
     "fbp_scan_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_scan_i32": (C.c_int, [_P, _P, _I64, _P, C.c_size_t, _P]),
     "fbp_scan_i32_noalloc": (C.c_int, [_P, _P, _I64, _P]),
-    "fbp_inside_count": (C.c_int, [_P, _I64, C.POINTER(Boxes), _P, _P, _P, _P, _P]),
-    "fbp_inside_fill": (C.c_int, [_P, _I64, C.POINTER(Boxes), _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P]),
+    "fbp_inside_count": (C.c_int, [_P, _I64, C.POINTER(Boxes), _P, _P, _P, _P, _P, _P, _P]),
+    "fbp_inside_fill": (C.c_int, [_P, _I64, C.POINTER(Boxes), _P, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P]),
     "fbp_gather_i32": (C.c_int, [_P, _I64, _P, _P, _P, _P]),
     "fbp_compact_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_compact_flags": (C.c_int, [_P, _I64, _P, _P, _P, C.c_size_t, _P]),

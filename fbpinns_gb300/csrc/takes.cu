@@ -43,7 +43,8 @@ __device__ __forceinline__ bool inside_box(const float* xp, const float* __restr
 template <int XD>
 __global__ void inside_count_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b,
                                     int32_t* __restrict__ pt_count, int32_t* __restrict__ pt_nlvl,
-                                    uint64_t* __restrict__ pt_lvl, int32_t* __restrict__ model_count) {
+                                    uint64_t* __restrict__ pt_lvl, int32_t* __restrict__ model_count,
+                                    uint64_t* __restrict__ pt_hit, int32_t* __restrict__ pt_cand) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
         float xp[XD];
@@ -52,24 +53,30 @@ __global__ void inside_count_kernel(const float* __restrict__ x, int64_t n, fbp_
         const int c = cell_of<XD>(xp, b);
         const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
         int cnt = 0;
-        uint64_t lvl = 0;
+        uint64_t lvl = 0, hit = 0;
         for (int e = e0; e < e1; ++e) {
             const int j = b.cell_boxes[e];
             if (b.select && !b.select[j]) continue;
             if (inside_box<XD>(xp, b.xmins, b.xmaxs, j)) {
                 ++cnt;
                 lvl |= 1ull << (b.pou[j] & 63);
+                if (e - e0 < 64) hit |= 1ull << (e - e0);
                 if (model_count) atomicAdd(&model_count[j], 1);
             }
         }
         pt_count[p] = cnt;
         if (pt_nlvl) pt_nlvl[p] = __popcll(lvl);
         if (pt_lvl) pt_lvl[p] = lvl;
+        // hits as a mask over the cell's candidate list (cells of <= 64 candidates)
+        if (pt_hit) pt_hit[p] = hit;
+        if (pt_cand) pt_cand[p] = e1 - e0 <= 64 ? e0 : -1;
     }
 }
 
-// Fill: one thread per point tests the candidates of its cell (the box arrays
-// are small and stay in L1); a warp's 32 consecutive points own one contiguous
+// Fill: one thread per point takes its hits from the count pass's candidate
+// mask (or, for cells of more than 64 candidates or without the mask, tests
+// the candidates again; the box arrays are small and stay in L1); a warp's 32
+// consecutive points own one contiguous
 // range of the point-major pair arrays, so their hits are staged in shared
 // memory and the warp writes the range out coalesced.  A warp whose range
 // exceeds its staging space writes its points' pairs directly.  A staged pair
@@ -83,6 +90,7 @@ template <int XD>
 __global__ void __launch_bounds__(FILL_WARPS * 32)
     inside_fill_kernel(const float* __restrict__ x, int64_t n, fbp_boxes b, const int32_t* __restrict__ pt_off,
                        const int32_t* __restrict__ np_off, const uint64_t* __restrict__ pt_lvl,
+                       const uint64_t* __restrict__ pt_hit, const int32_t* __restrict__ pt_cand,
                        int32_t* __restrict__ n_take, int32_t* __restrict__ m_take, int32_t* __restrict__ p_take,
                        int32_t* __restrict__ np_take, int64_t s_cap, int64_t u_cap, int32_t* __restrict__ status) {
     __shared__ int32_t stage[FILL_WARPS][FILL_STAGE];
@@ -108,16 +116,37 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
         s_lvl[w][lane] = lvl;
         s_ubase[w][lane] = ubase;
         if (valid) {
+            int cand = -1;
+            uint64_t hit = 0;
+            if (pt_hit && pt_cand) {
+                cand = pt_cand[p];
+                hit = pt_hit[p];
+            }
+            int e = 0, e1 = 0;
             float xp[XD];
+            if (cand < 0) {
 #pragma unroll
-            for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
-            const int c = cell_of<XD>(xp, b);
-            const int e0 = b.cell_start[c], e1 = b.cell_start[c + 1];
+                for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
+                const int c = cell_of<XD>(xp, b);
+                e = b.cell_start[c];
+                e1 = b.cell_start[c + 1];
+            }
             int64_t k = 0;
-            for (int e = e0; e < e1; ++e) {
-                const int j = b.cell_boxes[e];
-                if (b.select && !b.select[j]) continue;
-                if (!inside_box<XD>(xp, b.xmins, b.xmaxs, j)) continue;
+            for (;;) {
+                // next hit: from the mask, or by testing the next candidates
+                int j;
+                if (cand >= 0) {
+                    if (!hit) break;
+                    j = b.cell_boxes[cand + __ffsll((long long)hit) - 1];
+                    hit &= hit - 1;
+                } else {
+                    for (; e < e1; ++e) {
+                        j = b.cell_boxes[e];
+                        if ((!b.select || b.select[j]) && inside_box<XD>(xp, b.xmins, b.xmaxs, j)) break;
+                    }
+                    if (e >= e1) break;
+                    ++e;
+                }
                 const int lv = b.pou[j] & 63;
                 const int64_t q = base + k - wb;
                 if (staged) {
@@ -469,7 +498,8 @@ extern "C" int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* sc
 }
 
 extern "C" int fbp_inside_count(const float* x, int64_t n, const fbp_boxes* boxes, int32_t* pt_count,
-                                int32_t* pt_nlvl, uint64_t* pt_lvl, int32_t* model_count, void* stream) {
+                                int32_t* pt_nlvl, uint64_t* pt_lvl, int32_t* model_count, uint64_t* pt_hit,
+                                int32_t* pt_cand, void* stream) {
     int rc = check_boxes(boxes);
     if (rc) return rc;
     FBP_REQUIRE(pt_count && (x || n == 0), FBP_ERR_INVALID, "fbp_inside_count: null pointer");
@@ -477,16 +507,17 @@ extern "C" int fbp_inside_count(const float* x, int64_t n, const fbp_boxes* boxe
     const int g = grid_for(n, 256);
     cudaStream_t st = as_stream(stream);
     switch (boxes->xd) {
-        case 1: inside_count_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
-        case 2: inside_count_kernel<2><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
-        case 3: inside_count_kernel<3><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count); break;
+        case 1: inside_count_kernel<1><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count, pt_hit, pt_cand); break;
+        case 2: inside_count_kernel<2><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count, pt_hit, pt_cand); break;
+        case 3: inside_count_kernel<3><<<g, 256, 0, st>>>(x, n, *boxes, pt_count, pt_nlvl, pt_lvl, model_count, pt_hit, pt_cand); break;
     }
     FBP_LAUNCH_CHECK();
     return FBP_OK;
 }
 
 extern "C" int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes, const int32_t* pt_off,
-                               const int32_t* np_off, const uint64_t* pt_lvl, int32_t* n_take, int32_t* m_take,
+                               const int32_t* np_off, const uint64_t* pt_lvl, const uint64_t* pt_hit,
+                               const int32_t* pt_cand, int32_t* n_take, int32_t* m_take,
                                int32_t* p_take, int32_t* np_take, int64_t s_cap, int64_t u_cap, int32_t* status,
                                void* stream) {
     int rc = check_boxes(boxes);
@@ -499,9 +530,9 @@ extern "C" int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes
     const int g = grid_for(n, FILL_WARPS * 32, 8);  // 32 points per warp
     cudaStream_t st = as_stream(stream);
     switch (boxes->xd) {
-        case 1: inside_fill_kernel<1><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
-        case 2: inside_fill_kernel<2><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
-        case 3: inside_fill_kernel<3><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 1: inside_fill_kernel<1><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, pt_hit, pt_cand, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 2: inside_fill_kernel<2><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, pt_hit, pt_cand, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
+        case 3: inside_fill_kernel<3><<<g, FILL_WARPS * 32, 0, st>>>(x, n, *boxes, pt_off, np_off, pt_lvl, pt_hit, pt_cand, n_take, m_take, p_take, np_take, s_cap, u_cap, status); break;
     }
     FBP_LAUNCH_CHECK();
     return FBP_OK;

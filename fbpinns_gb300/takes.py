@@ -82,6 +82,10 @@ class PointTakes:
         self.pt_count = torch.zeros(self.n, dtype=torch.int32, device=dev)
         self.pt_nlvl = torch.zeros(self.n, dtype=torch.int32, device=dev)
         self.pt_lvl = torch.zeros(self.n, dtype=torch.int64, device=dev)
+        # hits of the count pass as candidate-list masks, read by the fill pass
+        self.pt_hit = torch.zeros(self.n, dtype=torch.int64, device=dev)
+        self.pt_cand = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        self.use_hit_masks = True
         self.pt_off = torch.zeros(self.n + 1, dtype=torch.int32, device=dev)
         self.np_off = torch.zeros(self.n + 1, dtype=torch.int32, device=dev)
         self.model_count = torch.zeros(grid.m, dtype=torch.int32, device=dev)
@@ -120,7 +124,8 @@ class PointTakes:
             self.model_count.zero_()
         _lib.check(lib.fbp_inside_count(_lib.ptr(x), self.n, C.byref(b), _lib.ptr(self.pt_count),
                                         _lib.ptr(self.pt_nlvl), _lib.ptr(self.pt_lvl),
-                                        _lib.ptr(self.model_count) if count_models else None, st),
+                                        _lib.ptr(self.model_count) if count_models else None,
+                                        _lib.ptr(self.pt_hit), _lib.ptr(self.pt_cand), st),
                    "fbp_inside_count")
         sb = self._scan_scratch.numel() * 4
         _lib.check(lib.fbp_scan_i32(_lib.ptr(self.pt_count), _lib.ptr(self.pt_off), self.n,
@@ -137,7 +142,10 @@ class PointTakes:
         else:
             s_cap, u_cap = self.n_take.numel(), self.np_take.numel()
         _lib.check(lib.fbp_inside_fill(_lib.ptr(x), self.n, C.byref(b), _lib.ptr(self.pt_off), _lib.ptr(self.np_off),
-                                       _lib.ptr(self.pt_lvl), _lib.ptr(self.n_take), _lib.ptr(self.m_take),
+                                       _lib.ptr(self.pt_lvl),
+                                       _lib.ptr(self.pt_hit) if self.use_hit_masks else None,
+                                       _lib.ptr(self.pt_cand) if self.use_hit_masks else None,
+                                       _lib.ptr(self.n_take), _lib.ptr(self.m_take),
                                        _lib.ptr(self.p_take), _lib.ptr(self.np_take), s_cap, u_cap,
                                        _lib.ptr(self.status), st), "fbp_inside_fill")
         self._sizes = sizes
@@ -184,7 +192,7 @@ def inside_models(static, x_batch, ims):
     st = _lib.stream_ptr()
     t.model_count.zero_()
     _lib.check(lib.fbp_inside_count(_lib.ptr(x), t.n, C.byref(b), _lib.ptr(t.pt_count), None, None,
-                                    _lib.ptr(t.model_count), st), "fbp_inside_count")
+                                    _lib.ptr(t.model_count), None, None, st), "fbp_inside_count")
     ips = compact_flags(t.pt_count)
     counts = t.model_count[ims].double()
     d = float(counts.mean() ** (1.0 / g.xd)) if ims.numel() else float("nan")

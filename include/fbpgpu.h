@@ -165,22 +165,30 @@ int fbp_scan_i32_noalloc(const int32_t* in, int32_t* out, int64_t n, void* strea
 /* Count pass of the point-in-box test.  For every point: the number of
  * selected boxes that contain it (pt_count), the bit mask of their POU levels
  * (pt_lvl) and its popcount (pt_nlvl).  model_count (nullable) receives the
- * number of points inside each box.  Replaces _inside_sum_batch
+ * number of points inside each box.  pt_hit / pt_cand (nullable, together)
+ * receive the hits as a bit mask over the point's cell candidate list and
+ * that list's start, or -1 when the cell has more than 64 candidates; the
+ * fill pass then reads the hits instead of testing again.
+ * Replaces _inside_sum_batch
  * (fbpinns/decompositions_base.py:24-48) as used by inside_points /
  * inside_models (fbpinns/decompositions.py:202-215). */
 int fbp_inside_count(const float* x, int64_t n, const fbp_boxes* boxes,
                      int32_t* pt_count, int32_t* pt_nlvl, uint64_t* pt_lvl,
-                     int32_t* model_count, void* stream);
+                     int32_t* model_count, uint64_t* pt_hit, int32_t* pt_cand,
+                     void* stream);
 
 /* Fill pass: writes the interaction lists in the reference's point-major,
  * box-minor order (n_take, m_take = box id) and the unique (point, level)
  * slots (p_take, np_take) in the order of
  * jnp.unique(stack(n_take, pou[m_take]), axis=0, return_inverse=True).
  * pt_off / np_off are the exclusive scans of pt_count / pt_nlvl (n+1 long).
+ * pt_hit / pt_cand: from fbp_inside_count on the same points and boxes
+ * (select included), or NULL to test the candidates again.
  * Replaces _inside_take_batch (fbpinns/decompositions_base.py:51-68) and the
  * POU unique of get_inputs (fbpinns/trainers.py:379-388). */
 int fbp_inside_fill(const float* x, int64_t n, const fbp_boxes* boxes,
                     const int32_t* pt_off, const int32_t* np_off, const uint64_t* pt_lvl,
+                    const uint64_t* pt_hit, const int32_t* pt_cand,
                     int32_t* n_take, int32_t* m_take, int32_t* p_take, int32_t* np_take,
                     int64_t s_cap, int64_t u_cap, int32_t* status, void* stream);
 

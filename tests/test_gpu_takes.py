@@ -74,6 +74,43 @@ def test_random_points_multilevel_vs_oracle(cuda, n, seed):
         np.testing.assert_array_equal(_np(takes[k]), ref[k])
 
 
+@pytest.mark.parametrize("dense", [False, True])
+def test_fill_hit_masks_match_testing_again(cuda, dense):
+    """The fill pass takes its hits from the count pass's candidate masks
+    (cells of <= 64 candidates) or tests the candidates again (denser cells, or
+    no masks passed): the lists are identical either way and match the oracle.
+    dense=True adds 80 boxes covering the whole domain, so every cell has more
+    than 64 candidates."""
+    rng = np.random.default_rng(9)
+    lo = rng.uniform(0, 0.9, (150, 2)).astype(np.float32)
+    hi = (lo + rng.uniform(0.05, 0.3, (150, 2))).astype(np.float32)
+    if dense:
+        lo = np.concatenate([lo, rng.uniform(-0.3, -0.06, (80, 2)).astype(np.float32)])
+        hi = np.concatenate([hi, rng.uniform(1.3, 1.5, (80, 2)).astype(np.float32)])
+    pou = (np.arange(lo.shape[0]) % 5).astype(np.float32)
+    st = boxes_static(lo, hi, pou)
+    x = rng.uniform(-0.05, 1.25, (5000, 2)).astype(np.float32)
+    g = T.grid_of(st)
+    xd = torch.tensor(x, device=g.device)
+    out = []
+    for masks in (True, False):
+        t = T.PointTakes(g, x.shape[0])
+        t.use_hit_masks = masks
+        s, u = t.build(xd)
+        t.check_status()
+        out.append([_np(a[:k]) for a, k in ((t.n_take, s), (t.m_take, s), (t.p_take, s), (t.np_take, u))])
+        if masks:
+            cand = _np(t.pt_cand)
+            assert (cand < 0).all() if dense else (cand >= 0).all()
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+    ref = OT.get_inputs(x, np.ones(lo.shape[0], dtype=int), lo, hi, pou.astype(np.int64))[0]
+    np.testing.assert_array_equal(out[0][1], ref[0])  # m_take
+    np.testing.assert_array_equal(out[0][0], ref[1])  # n_take
+    np.testing.assert_array_equal(out[0][2], ref[2])  # p_take
+    np.testing.assert_array_equal(out[0][3], ref[3])  # np_take
+
+
 def test_points_on_box_boundaries_3d(cuda):
     """Points exactly on box faces (closed boxes) and outside the decomposition."""
     static = decomposition("wave")
