@@ -439,14 +439,17 @@ __global__ void work_count_kernel(const int32_t* __restrict__ sd_start, int64_t 
     }
 }
 
+// one warp per subdomain: the lanes write its items (a subdomain holding all
+// points has hundreds of them)
 __global__ void work_fill_kernel(const int32_t* __restrict__ sd_start, int64_t m, const int32_t* __restrict__ ioff,
                                  int chunk, int32_t* __restrict__ items, int32_t* __restrict__ item_start,
                                  int32_t* __restrict__ n_items, int64_t cap, int32_t* __restrict__ status) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m;
-         j += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; j < m; j += nw) {
         const int i0 = ioff[j], i1 = ioff[j + 1];
         const int b = sd_start[j], e = sd_start[j + 1];
-        for (int it = i0; it < i1; ++it) {
+        for (int it = i0 + lane; it < i1; it += 32) {
             if (it >= cap) {
                 atomicOr(status, FBP_STATUS_ITEM_OVERFLOW);
                 break;
@@ -456,10 +459,12 @@ __global__ void work_fill_kernel(const int32_t* __restrict__ sd_start, int64_t m
             items[3 * (int64_t)it + 1] = beg;
             items[3 * (int64_t)it + 2] = min(chunk, e - beg);
         }
-        item_start[j] = min((int64_t)i0, cap);
-        if (j == m - 1) {
-            item_start[m] = min((int64_t)i1, cap);
-            *n_items = (int32_t)min((int64_t)i1, cap);
+        if (lane == 0) {
+            item_start[j] = min((int64_t)i0, cap);
+            if (j == m - 1) {
+                item_start[m] = min((int64_t)i1, cap);
+                *n_items = (int32_t)min((int64_t)i1, cap);
+            }
         }
     }
 }
@@ -639,7 +644,7 @@ extern "C" int fbp_build_work(const int32_t* sd_start, int64_t m, const uint8_t*
     FBP_LAUNCH_CHECK();
     int rc = scan_launch(nit, ioff, m, sums, st);
     if (rc) return rc;
-    work_fill_kernel<<<grid_for(m, 256), 256, 0, st>>>(sd_start, m, ioff, chunk, items, item_start, n_items,
+    work_fill_kernel<<<grid_for(m * 32, 256), 256, 0, st>>>(sd_start, m, ioff, chunk, items, item_start, n_items,
                                                         items_cap, status);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
