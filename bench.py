@@ -237,7 +237,9 @@ def run_fused(args, world, rank, local):
     seed = SEED + 1000 * rank
 
     tc = False if args.fma_forward else None
-    eng = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
+    # the Poisson residual needs only the Laplacian: jets (u, u_x, u_y, u_xx + u_yy)
+    d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
+    eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
@@ -273,7 +275,7 @@ def run_fused(args, world, rank, local):
     # ---- end to end through the public step API with host buffers ----------
     e2e = None
     try:
-        eng2 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -399,6 +401,7 @@ def run_fused(args, world, rank, local):
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
                            "parallelism": f"replicas x{world}", "chunk": args.chunk,
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
+                           "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
                                  ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
                 "e2e": e2e, "gpu_launches": per_step * args.steps, "clocks": clocks, "roofline": roofline,
@@ -416,6 +419,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=512)
     ap.add_argument("--grid", type=int, default=0)
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
+    ap.add_argument("--per-dim-jets", action="store_true",
+                    help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-timed", action="store_true",

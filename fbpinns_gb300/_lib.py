@@ -23,6 +23,7 @@ STATUS_BITS = {
 }
 
 PROBLEM_NONE, PROBLEM_HO_HARDBC, PROBLEM_BURGERS, PROBLEM_POISSON2D, PROBLEM_WAVE_C, PROBLEM_HELMHOLTZ2D = range(6)
+D2_LAPLACIAN = 8  # FBP_D2_LAPLACIAN: one jet slot for the sum of the masked second derivatives
 
 
 class FBPLibraryError(RuntimeError):

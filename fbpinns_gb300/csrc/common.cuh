@@ -42,8 +42,16 @@ __host__ __device__ constexpr int popc_const(int v) {
     return v == 0 ? 0 : (v & 1) + popc_const(v >> 1);
 }
 
-// Jet layout: [u, d/dx_0..d/dx_{XD-1}, d2/dx_i^2 for each bit i of D2 ascending].
-__host__ __device__ constexpr int jet_size(int xd, int d2) { return 1 + xd + popc_const(d2); }
+// Second-derivative part of a jet, from the d2mask: bits 0-2 name the dims
+// whose pure second derivatives are needed; with FBP_D2_LAPLACIAN (bit 3) set,
+// one slot holds their sum (the Laplacian over those dims, propagated directly
+// as in the forward-Laplacian scheme) instead of one slot per dim.
+__host__ __device__ constexpr bool d2_lap(int d2) { return (d2 & FBP_D2_LAPLACIAN) != 0; }
+__host__ __device__ constexpr int d2_slots(int d2) { return d2_lap(d2) ? ((d2 & 7) ? 1 : 0) : popc_const(d2 & 7); }
+
+// Jet layout: [u, d/dx_0..d/dx_{XD-1}, then the second-derivative slots: one
+// per bit i of the d2mask ascending, or the single Laplacian slot].
+__host__ __device__ constexpr int jet_size(int xd, int d2) { return 1 + xd + d2_slots(d2); }
 
 // Index of the s-th set bit of mask among bits 0..7 (0 when there is none).
 __host__ __device__ constexpr int nth_bit(int mask, int s) {
@@ -68,6 +76,13 @@ struct DimsOf {
     __host__ __device__ static constexpr int get(int s) { return s == 0 ? d0 : (s == 1 ? d1 : d2); }
 };
 
+// Dims whose pure second derivatives second-derivative slot s of a d2mask sums
+// (one dim per slot, or all masked dims for the Laplacian slot).
+template <int D2>
+__host__ __device__ constexpr int d2_slot_dims(int s) {
+    return d2_lap(D2) ? (D2 & 7) : (1 << DimsOf<D2 & 7>::get(s));
+}
+
 // tanh from the identity tanh|x| = (1 - e) / (1 + e), e = exp(-2|x|), with the
 // __expf / __fdividef intrinsics and the sign restored.  e lies in (0, 1], so
 // nothing overflows; the absolute error is about 1e-7 over the whole line
@@ -80,6 +95,7 @@ __device__ __forceinline__ float tanh_fast(float x) {
 inline int jet_size_rt(int xd, int d2) {
     int c = 0;
     for (int i = 0; i < xd; ++i) c += (d2 >> i) & 1;
+    if (d2_lap(d2)) c = c ? 1 : 0;
     return 1 + xd + c;
 }
 

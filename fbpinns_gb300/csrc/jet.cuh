@@ -20,7 +20,7 @@ namespace fbp {
 template <int XD_, int H1_, int H2_, int D2_>
 struct Cfg {
     static constexpr int XD = XD_, H1 = H1_, H2 = H2_, D2 = D2_;
-    static constexpr int NS = popc_const(D2);
+    static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
     static constexpr bool TWO = H2 > 0;
     static constexpr int HL = TWO ? H2 : H1;  // width feeding the output layer
@@ -34,7 +34,8 @@ struct Cfg {
     static constexpr int NCH = TWO ? H2 / KC : 1;
     static_assert(!TWO || H2 % KC == 0, "H2 must be a multiple of the chunk");
     // second-derivative dim of slot s
-    __host__ __device__ static constexpr int sd_dim(int s) { return DimsOf<D2>::get(s); }
+    // dims whose pure second derivatives slot s sums
+    __host__ __device__ static constexpr int slot_dims(int s) { return d2_slot_dims<D2>(s); }
 };
 
 // the sorted pair record (point-major pair index, point, slot, 0)
@@ -47,7 +48,7 @@ struct SParams {
     float W1[C::H1 * C::XD];
     float b1[C::H1];
     float cw[C::H1 * C::XD];   // W1[n][d] / sd[d]: first-layer tangent along d
-    float cw2[C::H1 * C::XD];  // cw^2
+    float c2[C::H1 * (C::NS > 0 ? C::NS : 1)];  // per slot s: sum of cw[n][d]^2 over its dims
     float W2t[C::TWO ? C::H1 * C::H2 : 4];  // [n][k]
     float W2[C::TWO ? C::H2 * C::H1 : 4];   // [k][n]
     float b2[C::TWO ? C::H2 : 4];
@@ -89,11 +90,20 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
     __syncthreads();
     for (int i = threadIdx.x; i < C::H1 * C::XD; i += blockDim.x) {
         const int d = i % C::XD;
-        const float c = S.W1[i] * S.inv_sd[d];
-        S.cw[i] = c;
-        S.cw2[i] = c * c;
+        S.cw[i] = S.W1[i] * S.inv_sd[d];
     }
     __syncthreads();
+    if constexpr (C::NS > 0) {
+        for (int i = threadIdx.x; i < C::H1 * C::NS; i += blockDim.x) {
+            const int n = i / C::NS, s = i - n * C::NS;
+            float v = 0.f;
+#pragma unroll
+            for (int d = 0; d < C::XD; ++d)
+                if ((C::slot_dims(s) >> d) & 1) v = fmaf(S.cw[n * C::XD + d], S.cw[n * C::XD + d], v);
+            S.c2[i] = v;
+        }
+        __syncthreads();
+    }
 }
 
 // Jet of one first-layer neuron's activation from a = tanh(z1).
@@ -104,7 +114,7 @@ __device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, floa
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) v[1 + d] = tp * S.cw[n * C::XD + d];
 #pragma unroll
-    for (int s = 0; s < C::NS; ++s) v[1 + C::XD + s] = tpp * S.cw2[n * C::XD + C::sd_dim(s)];
+    for (int s = 0; s < C::NS; ++s) v[1 + C::XD + s] = tpp * S.c2[n * C::NS + s];
 }
 
 // tanh applied to a z-jet.
@@ -119,8 +129,11 @@ __device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J
     for (int d = 0; d < C::XD; ++d) g[1 + d] = tp * z[1 + d];
 #pragma unroll
     for (int s = 0; s < C::NS; ++s) {
-        const float zd = z[1 + C::sd_dim(s)];
-        g[1 + C::XD + s] = tp * z[1 + C::XD + s] + tpp * zd * zd;
+        float q = 0.f;
+#pragma unroll
+        for (int d = 0; d < C::XD; ++d)
+            if ((C::slot_dims(s) >> d) & 1) q = fmaf(z[1 + d], z[1 + d], q);
+        g[1 + C::XD + s] = tp * z[1 + C::XD + s] + tpp * q;
     }
 }
 
@@ -136,12 +149,16 @@ __device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float a, fl
     }
 #pragma unroll
     for (int s = 0; s < C::NS; ++s) {
-        const int d = C::sd_dim(s);
         const float g = gb[1 + C::XD + s];
         tpb += g * z[1 + C::XD + s];
-        tppb += g * z[1 + d] * z[1 + d];
         zb[1 + C::XD + s] = g * tp;
-        zb[1 + d] += 2.0f * g * tpp * z[1 + d];
+        const float g2 = 2.0f * g * tpp;
+#pragma unroll
+        for (int d = 0; d < C::XD; ++d)
+            if ((C::slot_dims(s) >> d) & 1) {
+                tppb += g * z[1 + d] * z[1 + d];
+                zb[1 + d] += g2 * z[1 + d];
+            }
     }
     const float ab = gb[0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f);
     zb[0] = ab * tp;
@@ -177,12 +194,53 @@ __device__ __forceinline__ void window_jet(const SParams<C>& S, const float (&xn
     }
 #pragma unroll
     for (int s = 0; s < C::NS; ++s) {
-        const int i = C::sd_dim(s);
-        float p = c2[i];
+        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < C::XD; ++i)
+            if ((C::slot_dims(s) >> i) & 1) {
+                float p = c2[i];
+#pragma unroll
+                for (int d = 0; d < C::XD; ++d)
+                    if (d != i) p *= c0[d];
+                acc += p;
+            }
+        w[1 + C::XD + s] = f * acc;
+    }
+}
+
+// Jet of the product u w (first J entries of a pair record).
+template <class C>
+__device__ __forceinline__ void product_jet(const float (&u)[C::J], const float (&w)[C::J], float* rec) {
+    rec[0] = u[0] * w[0];
+#pragma unroll
+    for (int d = 0; d < C::XD; ++d) rec[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
+#pragma unroll
+    for (int s = 0; s < C::NS; ++s) {
+        float v = u[1 + C::XD + s] * w[0] + u[0] * w[1 + C::XD + s];
 #pragma unroll
         for (int d = 0; d < C::XD; ++d)
-            if (d != i) p *= c0[d];
-        w[1 + C::XD + s] = f * p;
+            if ((C::slot_dims(s) >> d) & 1) v += 2.0f * u[1 + d] * w[1 + d];
+        rec[1 + C::XD + s] = v;
+    }
+}
+
+// Adjoint of product_jet in u with w fixed: u-bar = M_w^T n-bar.
+template <class C>
+__device__ __forceinline__ void product_jet_adj(const float (&nb)[C::J], const float (&w)[C::J], float (&ub)[C::J]) {
+    ub[0] = nb[0] * w[0];
+#pragma unroll
+    for (int d = 0; d < C::XD; ++d) {
+        ub[0] += nb[1 + d] * w[1 + d];
+        ub[1 + d] = nb[1 + d] * w[0];
+    }
+#pragma unroll
+    for (int s = 0; s < C::NS; ++s) {
+        const float g = nb[1 + C::XD + s];
+        ub[0] += g * w[1 + C::XD + s];
+#pragma unroll
+        for (int d = 0; d < C::XD; ++d)
+            if ((C::slot_dims(s) >> d) & 1) ub[1 + d] += 2.0f * g * w[1 + d];
+        ub[1 + C::XD + s] = g * w[0];
     }
 }
 
@@ -312,14 +370,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net n
             float w[J];
             window_jet<C>(S, xn, w);
             float rec[RS];
-            rec[0] = u[0] * w[0];
-#pragma unroll
-            for (int d = 0; d < XD; ++d) rec[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
-#pragma unroll
-            for (int s = 0; s < C::NS; ++s) {
-                const int d = C::sd_dim(s);
-                rec[1 + XD + s] = u[1 + XD + s] * w[0] + 2.0f * u[1 + d] * w[1 + d] + u[0] * w[1 + XD + s];
-            }
+            product_jet<C>(u, w, rec);
 #pragma unroll
             for (int c = 0; c < J; ++c) rec[J + c] = w[c];
 #pragma unroll
@@ -457,22 +508,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                     for (int c = 0; c < J; ++c) nb[c] = ok ? rec[c] : 0.f;
                 }
-                // adjoint of uw = u (*) w with w constant: u-bar = M_w^T N-bar
+                // adjoint of uw = u (*) w with w constant
                 float ub[J];
-                ub[0] = nb[0] * w[0];
-#pragma unroll
-                for (int d = 0; d < XD; ++d) {
-                    ub[0] += nb[1 + d] * w[1 + d];
-                    ub[1 + d] = nb[1 + d] * w[0];
-                }
-#pragma unroll
-                for (int s = 0; s < C::NS; ++s) {
-                    const int d = C::sd_dim(s);
-                    const float g = nb[1 + XD + s];
-                    ub[0] += g * w[1 + XD + s];
-                    ub[1 + d] += 2.0f * g * w[1 + d];
-                    ub[1 + XD + s] = g * w[0];
-                }
+                product_jet_adj<C>(nb, w, ub);
 #pragma unroll
                 for (int c = 0; c < J; ++c) ob[c] = ub[c] * S.sd_u;
 #pragma unroll 4
@@ -595,11 +633,11 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                         }
 #pragma unroll
                         for (int s = 0; s < C::NS; ++s) {
-                            const int d = C::sd_dim(s);
                             const float g = vb[q][1 + XD + s];
-                            const float cwd = S.cw[n * XD + d];
-                            tppb += g * cwd * cwd;
-                            cwb[d] += 2.0f * g * tpp * cwd;
+                            tppb += g * S.c2[n * C::NS + s];
+#pragma unroll
+                            for (int d = 0; d < XD; ++d)
+                                if ((C::slot_dims(s) >> d) & 1) cwb[d] += 2.0f * g * tpp * S.cw[n * XD + d];
                         }
                         const float z1b = (vb[q][0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f)) * tp;
 #pragma unroll
@@ -674,7 +712,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                 for (int d = 0; d < XD; ++d) v = fmaf(S.cw[n * XD + d], sacc[i][q][1 + d], v);
 #pragma unroll
                                 for (int ss = 0; ss < C::NS; ++ss)
-                                    v = fmaf(S.cw2[n * XD + C::sd_dim(ss)], sacc[i][q][1 + XD + ss], v);
+                                    v = fmaf(S.c2[n * C::NS + ss], sacc[i][q][1 + XD + ss], v);
                                 R.gW2[(k0 + i) * H1 + n] += v;
                             }
                         if (nb == 0) {

@@ -11,6 +11,7 @@ int jet_group_a(int mode, const fbp_net* net, const float* x, const fbp_pairs* p
     FBP_TRY(2, 16, 16, 1)
     FBP_TRY(2, 16, 16, 0)
     FBP_TRY(2, 16, 0, 1)
+    FBP_TRY(2, 16, 16, 11)  // Laplacian slot (Poisson)
     return 1;
 }
 }  // namespace fbp

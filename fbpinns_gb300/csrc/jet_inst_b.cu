@@ -9,6 +9,8 @@ int jet_group_b(int mode, const fbp_net* net, const float* x, const fbp_pairs* p
     FBP_TRY(2, 32, 32, 0)
     FBP_TRY(2, 8, 8, 3)
     FBP_TRY(2, 8, 8, 1)
+    FBP_TRY(2, 32, 32, 11)  // Laplacian slot (Helmholtz)
+    FBP_TRY(2, 8, 8, 11)
     return 1;
 }
 }  // namespace fbp

@@ -53,6 +53,8 @@ extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fb
                 "fbp_forward_pairs_tc: only the xd-16-16-1 networks are compiled (got h1=%d h2=%d ud=%d)", net->h1,
                 net->h2, net->ud);
     cudaStream_t st = fbp::as_stream(stream);
+    if (net->xd == 2 && net->d2mask == (3 | FBP_D2_LAPLACIAN))
+        return fbp::launch_forward_tc<2, 3 | FBP_D2_LAPLACIAN>(*net, x, *pairs, pair_out, status, grid, st);
     if (net->xd == 2 && net->d2mask == 3) return fbp::launch_forward_tc<2, 3>(*net, x, *pairs, pair_out, status, grid, st);
     if (net->xd == 2 && net->d2mask == 1) return fbp::launch_forward_tc<2, 1>(*net, x, *pairs, pair_out, status, grid, st);
     if (net->xd == 2 && net->d2mask == 0) return fbp::launch_forward_tc<2, 0>(*net, x, *pairs, pair_out, status, grid, st);

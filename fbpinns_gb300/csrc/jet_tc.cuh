@@ -4,9 +4,10 @@
 // Layer 2 of the jet, z_c[k] = sum_n W2[k][n] v_c[n] (+ b2[k] for c = 0), is
 // J small GEMMs per tile of 128 pairs (M = 128 pairs, N = 16, K = 16).  The
 // layer-1 jet components factor as v_0 = a, v_{1+d} = tp * cw[:, d] and
-// v_{1+xd+s} = tpp * cw2[:, d_s] (tp = 1 - a^2, tpp = -2 a tp, cw = W1 / sd),
+// v_{1+xd+s} = tpp * c2_s (tp = 1 - a^2, tpp = -2 a tp, cw = W1 / sd, c2_s the
+// sum of cw[:, d]^2 over the dims of second-derivative slot s),
 // so the pair-dependent A operands are only a, tp and tpp, and the per-neuron
-// scale moves into B: B_c = W2 diag(f_c), f_c = 1, cw[:, d] or cw2[:, d_s],
+// scale moves into B: B_c = W2 diag(f_c), f_c = 1, cw[:, d] or c2_s,
 // built once per work item.  Each thread writes its pair's rows of a, tp, tpp
 // into shared memory, split as v = hi + lo with hi = v truncated to TF32, in
 // the no-swizzle K-major layout of 8-row x 16-byte core matrices; one thread
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             const int k = r / H1, n = r - k * H1;
             float f = 1.0f;
             if (c >= 1 && c <= XD) f = S.cw[n * XD + (c - 1)];
-            if (c > XD) f = S.cw2[n * XD + C::sd_dim(c - 1 - XD)];
+            if (c > XD) f = S.c2[n * C::NS + (c - 1 - XD)];
             float hi, lo;
             split_tf32(S.W2[r] * f, hi, lo);
             const uint32_t off = kmajor16_off(k, n) >> 2;
@@ -288,14 +289,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
                 for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
                 u[0] += S.mu_u;
                 float rec[RS];
-                rec[0] = u[0] * w[0];
-#pragma unroll
-                for (int d = 0; d < XD; ++d) rec[1 + d] = u[1 + d] * w[0] + u[0] * w[1 + d];
-#pragma unroll
-                for (int s = 0; s < C::NS; ++s) {
-                    const int d = C::sd_dim(s);
-                    rec[1 + XD + s] = u[1 + XD + s] * w[0] + 2.0f * u[1 + d] * w[1 + d] + u[0] * w[1 + XD + s];
-                }
+                product_jet<C>(u, w, rec);
 #pragma unroll
                 for (int c = 0; c < J; ++c) rec[J + c] = w[c];
 #pragma unroll

@@ -18,14 +18,19 @@ namespace fbp {
 
 template <int XD, int D2>
 struct JL {
-    static constexpr int NS = popc_const(D2);
+    static constexpr bool LAP = d2_lap(D2);
+    static constexpr int M = D2 & 7;
+    static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
-    __host__ __device__ static constexpr int dim(int s) { return DimsOf<D2>::get(s); }
-    // component of the pure second derivative along d (-1 if absent)
-    static constexpr int S0 = ((D2 >> 0) & 1) ? 1 + XD : -1;
-    static constexpr int S1 = ((D2 >> 1) & 1) ? 1 + XD + popc_const(D2 & 1) : -1;
-    static constexpr int S2 = ((D2 >> 2) & 1) ? 1 + XD + popc_const(D2 & 3) : -1;
+    // dims whose pure second derivatives slot s sums
+    __host__ __device__ static constexpr int slot_dims(int s) { return d2_slot_dims<D2>(s); }
+    // component of the pure second derivative along d (-1 if absent or summed)
+    static constexpr int S0 = (!LAP && ((M >> 0) & 1)) ? 1 + XD : -1;
+    static constexpr int S1 = (!LAP && ((M >> 1) & 1)) ? 1 + XD + popc_const(M & 1) : -1;
+    static constexpr int S2 = (!LAP && ((M >> 2) & 1)) ? 1 + XD + popc_const(M & 3) : -1;
     __host__ __device__ static constexpr int sidx(int d) { return d == 0 ? S0 : (d == 1 ? S1 : S2); }
+    // component of the Laplacian over the masked dims (-1 without FBP_D2_LAPLACIAN)
+    static constexpr int LAPI = (LAP && M) ? 1 + XD : -1;
 };
 
 template <int XD, int D2>
@@ -38,8 +43,11 @@ __device__ __forceinline__ void quotient(const float (&N)[JL<XD, D2>::J], const 
     for (int d = 0; d < XD; ++d) U[1 + d] = (N[1 + d] - U[0] * W[1 + d]) * r;
 #pragma unroll
     for (int s = 0; s < L::NS; ++s) {
-        const int d = L::dim(s);
-        U[1 + XD + s] = (N[1 + XD + s] - 2.0f * U[1 + d] * W[1 + d] - U[0] * W[1 + XD + s]) * r;
+        float v = N[1 + XD + s] - U[0] * W[1 + XD + s];
+#pragma unroll
+        for (int d = 0; d < XD; ++d)
+            if ((L::slot_dims(s) >> d) & 1) v -= 2.0f * U[1 + d] * W[1 + d];
+        U[1 + XD + s] = v * r;
     }
 }
 
@@ -55,10 +63,11 @@ __device__ __forceinline__ void quotient_adj(const float (&W)[JL<XD, D2>::J], co
     float u0 = Ub[0];
 #pragma unroll
     for (int s = 0; s < L::NS; ++s) {
-        const int d = L::dim(s);
         const float g = Ub[1 + XD + s];
         Nb[1 + XD + s] = g * r;
-        ud[d] -= 2.0f * g * W[1 + d] * r;
+#pragma unroll
+        for (int d = 0; d < XD; ++d)
+            if ((L::slot_dims(s) >> d) & 1) ud[d] -= 2.0f * g * W[1 + d] * r;
         u0 -= g * W[1 + XD + s] * r;
     }
 #pragma unroll
@@ -102,12 +111,17 @@ __device__ __forceinline__ void sep_jet(const J1 (&f)[XD], float (&B)[JL<XD, D2>
     }
 #pragma unroll
     for (int s = 0; s < L::NS; ++s) {
-        const int i = L::dim(s);
-        float q = f[i].dd;
+        float acc = 0.f;
 #pragma unroll
-        for (int d = 0; d < XD; ++d)
-            if (d != i) q *= f[d].v;
-        B[1 + XD + s] = q;
+        for (int i = 0; i < XD; ++i)
+            if ((L::slot_dims(s) >> i) & 1) {
+                float q = f[i].dd;
+#pragma unroll
+                for (int d = 0; d < XD; ++d)
+                    if (d != i) q *= f[d].v;
+                acc += q;
+            }
+        B[1 + XD + s] = acc;
     }
 }
 
@@ -226,6 +240,15 @@ __device__ __forceinline__ float residual(const fbp_problem& P, const float* xp,
             break;
         }
         case FBP_PROBLEM_POISSON2D: {  // u_xx + u_yy + f
+            if constexpr (XD == 2 && L::LAPI > 0 && L::M == 3) {
+                float f = 0.f;
+                for (int k = 1; k <= P.n_int; ++k) {
+                    const float a = (float)(1 << k);
+                    f += 2.0f * a * 9.869604401089358f * sinpif(a * xp[0]) * sinpif(a * xp[1]);
+                }
+                r = u[L::LAPI] + f;
+                dr[L::LAPI] = 1.f;
+            }
             if constexpr (XD == 2 && L::sidx(0) > 0 && L::sidx(1) > 0) {
                 float f = 0.f;
                 for (int k = 1; k <= P.n_int; ++k) {
@@ -239,6 +262,18 @@ __device__ __forceinline__ float residual(const fbp_problem& P, const float* xp,
             break;
         }
         case FBP_PROBLEM_HELMHOLTZ2D: {  // u_xx + u_yy + k^2 u + f
+            if constexpr (XD == 2 && L::LAPI > 0 && L::M == 3) {
+                const float k = P.p[1];
+                float f = 0.f;
+                for (int g = 0; g < P.ng; ++g) {
+                    const float mx = P.gauss[4 * g], my = P.gauss[4 * g + 1], s = P.gauss[4 * g + 2], amp = P.gauss[4 * g + 3];
+                    const float dx = xp[0] - mx, dy = xp[1] - my;
+                    f += amp * expf(-0.5f * (dx * dx + dy * dy) / (s * s));
+                }
+                r = u[L::LAPI] + k * k * u[0] + f;
+                dr[L::LAPI] = 1.f;
+                dr[0] = k * k;
+            }
             if constexpr (XD == 2 && L::sidx(0) > 0 && L::sidx(1) > 0) {
                 const float k = P.p[1];
                 float f = 0.f;
@@ -419,8 +454,11 @@ __global__ void __launch_bounds__(POU_T) pou_loss_kernel(fbp_problem P, int64_t 
         for (int d = 0; d < XD; ++d) uc[1 + d] = A[1 + d] + B[1 + d] * u[0] + B[0] * u[1 + d];
 #pragma unroll
         for (int s = 0; s < JL<XD, D2>::NS; ++s) {
-            const int d = JL<XD, D2>::dim(s);
-            uc[1 + XD + s] = A[1 + XD + s] + B[1 + XD + s] * u[0] + 2.0f * B[1 + d] * u[1 + d] + B[0] * u[1 + XD + s];
+            float v = A[1 + XD + s] + B[1 + XD + s] * u[0] + B[0] * u[1 + XD + s];
+#pragma unroll
+            for (int d = 0; d < XD; ++d)
+                if ((JL<XD, D2>::slot_dims(s) >> d) & 1) v += 2.0f * B[1 + d] * u[1 + d];
+            uc[1 + XD + s] = v;
         }
         if (U_out) {
 #pragma unroll
@@ -442,9 +480,10 @@ __global__ void __launch_bounds__(POU_T) pou_loss_kernel(fbp_problem P, int64_t 
         }
 #pragma unroll
         for (int s = 0; s < JL<XD, D2>::NS; ++s) {
-            const int d = JL<XD, D2>::dim(s);
             ub[0] += B[1 + XD + s] * ucb[1 + XD + s];
-            ub[1 + d] += 2.0f * B[1 + d] * ucb[1 + XD + s];
+#pragma unroll
+            for (int d = 0; d < XD; ++d)
+                if ((JL<XD, D2>::slot_dims(s) >> d) & 1) ub[1 + d] += 2.0f * B[1 + d] * ucb[1 + XD + s];
             ub[1 + XD + s] = B[0] * ucb[1 + XD + s];
         }
         PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out, u_cap);
@@ -479,7 +518,8 @@ template <template <int, int> class K>
 struct XDispatch;
 
 #define FBP_XD_D2_CASES(X) \
-    X(1, 0) X(1, 1) X(2, 0) X(2, 1) X(2, 2) X(2, 3) X(3, 0) X(3, 1) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6) X(3, 7)
+    X(1, 0) X(1, 1) X(2, 0) X(2, 1) X(2, 2) X(2, 3) X(2, 11) X(3, 0) X(3, 1) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6) \
+        X(3, 7)
 
 static int grid_pts(int64_t n) {
     int64_t b = (n + POU_T - 1) / POU_T;

@@ -68,11 +68,23 @@ def jet_index(xd, d2mask, ixs):
         return 0
     if len(ixs) == 1:
         return 1 + ixs[0]
+    if d2mask & _lib.D2_LAPLACIAN:
+        raise ValueError("a Laplacian jet (FBP_D2_LAPLACIAN) holds no single second derivative")
     d = ixs[0]
     return 1 + xd + bin(d2mask & ((1 << d) - 1)).count("1")
 
 
+def laplacian_index(xd, d2mask):
+    """Component holding the sum of the masked pure second derivatives, for a
+    d2mask with FBP_D2_LAPLACIAN."""
+    if not d2mask & _lib.D2_LAPLACIAN or not d2mask & 7:
+        raise ValueError(f"d2mask {d2mask} has no Laplacian slot")
+    return 1 + xd
+
+
 def jet_size(xd, d2mask):
+    if d2mask & _lib.D2_LAPLACIAN:
+        return 1 + xd + (1 if d2mask & 7 else 0)
     return 1 + xd + bin(d2mask).count("1")
 
 

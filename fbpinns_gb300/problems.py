@@ -332,7 +332,8 @@ class Poisson2D(Problem):
     @classmethod
     def fused_spec(cls, all_params):
         p = all_params["static"]["problem"]
-        return {"kind": _lib.PROBLEM_POISSON2D, "p": [p["sd"]], "n_int": p["n_freq"], "gauss": None}
+        return {"kind": _lib.PROBLEM_POISSON2D, "p": [p["sd"]], "n_int": p["n_freq"], "gauss": None,
+                "laplacian": True}
 
 
 def seeded_gaussians(n, seed, centre=(0.1, 0.9), width=(0.02, 0.1), amp=(-1.0, 1.0)):
@@ -376,4 +377,5 @@ class Helmholtz2D(Problem):
     @classmethod
     def fused_spec(cls, all_params):
         p = all_params["static"]["problem"]
-        return {"kind": _lib.PROBLEM_HELMHOLTZ2D, "p": [p["sd"], p["k"]], "n_int": 0, "gauss": p["source"]}
+        return {"kind": _lib.PROBLEM_HELMHOLTZ2D, "p": [p["sd"], p["k"]], "n_int": 0, "gauss": p["source"],
+                "laplacian": True}

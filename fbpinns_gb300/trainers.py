@@ -261,6 +261,14 @@ class FBPINNTrainer:
         required = [con[-1] for con in constraints_global]
         constraints_global = [con[:-1] for con in constraints_global]
         d2 = d2mask_of(required, xd)
+        if c.engine not in ("fused", "generic", "plain"):
+            raise ValueError(f"engine must be 'fused', 'generic' or 'plain', not {c.engine!r}")
+        spec = problem.fused_spec(all_params) if c.engine == "fused" else None
+        single = len(constraints_global) == 1 and not all_params["trainable"].get("problem")
+        use_fused = spec is not None and single
+        if use_fused and spec.get("laplacian") and d2 and _lib.load().fbp_has_shape(
+                xd, layer_sizes[1], layer_sizes[2] if len(layer_sizes) == 4 else 0, d2 | _lib.D2_LAPLACIAN):
+            d2 |= _lib.D2_LAPLACIAN  # the residual needs only the Laplacian: one jet slot for it
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
                            tensor_cores=getattr(c, "tensor_cores", None))
         eng.set_theta(pack_layers(net_tr["layers"]))
@@ -268,11 +276,6 @@ class FBPINNTrainer:
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()
         all_params["static"]["problem"] = {k: _to_dev(v, dev) for k, v in all_params["static"]["problem"].items()}
         opt = c.optimiser(**c.optimiser_kwargs)
-        if c.engine not in ("fused", "generic", "plain"):
-            raise ValueError(f"engine must be 'fused', 'generic' or 'plain', not {c.engine!r}")
-        spec = problem.fused_spec(all_params) if c.engine == "fused" else None
-        single = len(constraints_global) == 1 and not all_params["trainable"].get("problem")
-        use_fused = spec is not None and single
         use_plain = c.engine == "plain"
         if use_plain and not single:
             raise NotImplementedError("the plain step handles one constraint without trainable problem params")

@@ -48,6 +48,12 @@ extern "C" {
 #define FBP_ERR_UNSUPPORTED (-3)  /* configuration with no compiled kernel */
 #define FBP_ERR_CAPACITY (-4)     /* caller buffer too small */
 
+/* d2mask flag: the second-derivative dims (bits 0-2) are carried as ONE jet
+ * slot holding the sum of their pure second derivatives (a Laplacian),
+ * instead of one slot per dim.  Enough for residuals that use only that sum
+ * (Poisson, Helmholtz); the jet then has 1 + xd + 1 components. */
+#define FBP_D2_LAPLACIAN 8
+
 /* Device status word bits (written by kernels into an int32 the caller owns). */
 #define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */
 #define FBP_STATUS_SLOT_OVERFLOW 2      /* more (point, level) slots than capacity */

@@ -20,6 +20,7 @@ from oracle import takes as OT
 from fbpinns_gb300.engine import FBPINNEngine, FBPINNJet, constrained_jets, jet_index, d2mask_of
 from fbpinns_gb300.networks import pack_layers
 from fbpinns_gb300 import problems as PR
+from fbpinns_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
@@ -101,8 +102,12 @@ def _oracle_loss_grad(name, static, layers64, x, prob_static):
     return loss.item(), gpack, a_ims, active
 
 
-@pytest.mark.parametrize("name", ["ho_hardbc", "burgers", "poisson", "wave", "helmholtz"])
-def test_fused_loss_and_gradient_vs_oracle(cuda, name):
+@pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("burgers", False), ("poisson", False),
+                                      ("poisson", True), ("wave", False), ("helmholtz", False),
+                                      ("helmholtz", True)])
+def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
+    """Fused loss and per-subdomain gradients vs the float64 oracle.  lap=True
+    carries one Laplacian jet slot (u_xx + u_yy) instead of u_xx and u_yy."""
     recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
     static = decomposition(recipe)
     layers64 = random_layers(ls, static["m"], seed=5)
@@ -111,7 +116,7 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name):
     prob_static = pcls.init_params(**pkw)[0]
     loss_ref, g_ref, a_ims, active = _oracle_loss_grad(name, static, layers32, x, prob_static)
     assert d2mask_of([_required(name)], x.shape[1]) | d2 == d2
-    eng = _engine(static, layers32, d2)
+    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0))
     eng.set_state(active)
     eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
     ps = eng.points(torch.tensor(x))
@@ -123,6 +128,25 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name):
     assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
     inactive = np.setdiff1d(np.arange(static["m"]), a_ims)
     assert np.all(grad[inactive] == 0)
+
+
+def test_laplacian_jets_match_sum_of_second_derivatives(cuda):
+    """A Laplacian jet (FBP_D2_LAPLACIAN) equals u_xx + u_yy of the per-dim
+    jet; value and gradient components agree too (FP32 rounding only)."""
+    static = decomposition("poisson")
+    for ls in ([2, 16, 16, 1], [2, 32, 32, 1], [2, 8, 8, 1]):
+        layers = random_layers(ls, static["m"], seed=21)
+        x = torch.tensor(_points("poisson", 5000, 3))
+        Us = []
+        for d2 in (3, 3 | _lib.D2_LAPLACIAN):
+            eng = _engine(static, layers, d2)
+            ps = eng.points(x)
+            Us.append(FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy())
+        U, L = Us
+        assert L.shape[1] == 4 and U.shape[1] == 5
+        for c in range(3):
+            assert rel_err(L[:, c], U[:, c]) < JET_TOL, (ls, c)
+        assert rel_err(L[:, 3], U[:, 3] + U[:, 4]) < JET_TOL, ls
 
 
 def test_generic_path_matches_fused(cuda):

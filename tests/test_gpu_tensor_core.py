@@ -52,9 +52,10 @@ def _check(ref, tc, J):
         assert err <= TC_TOL * max(scale, 1e-30), (c, err, scale)
 
 
-@pytest.mark.parametrize("d2", [3, 1, 0])
+@pytest.mark.parametrize("d2", [3, 1, 0, 3 | 8])
 def test_tensor_core_forward_matches_fma_small(cuda, d2):
-    """Four-level decomposition (85 subdomains), 3000 points, all three jet masks."""
+    """Four-level decomposition (85 subdomains), 3000 points, all compiled jet
+    masks (3 | 8: one Laplacian slot)."""
     ref, tc, J = _records("multilevel", d2, 3000, seed=5 + d2)
     _check(ref, tc, J)
 
