@@ -58,7 +58,9 @@ struct SParams {
     float flag, mu_u, sd_u;
 };
 
-template <class C>
+// Subdomain j's weights into shared memory (W2T: also the transposed W2 that
+// the CUDA-core layer-2 loops read).
+template <class C, bool W2T = true>
 __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, int j) {
     const float* __restrict__ th = net.theta + (size_t)j * C::P;
     for (int i = threadIdx.x; i < C::H1 * C::XD; i += blockDim.x) S.W1[i] = th[C::oW1 + i];
@@ -68,7 +70,7 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
             const float v = th[C::oW2 + i];
             const int k = i / C::H1, n = i - k * C::H1;
             S.W2[i] = v;
-            S.W2t[n * C::H2 + k] = v;
+            if constexpr (W2T) S.W2t[n * C::H2 + k] = v;
         }
         for (int i = threadIdx.x; i < C::H2; i += blockDim.x) S.b2[i] = th[C::ob2 + i];
     }
@@ -430,11 +432,15 @@ struct __align__(16) WarpRows {
 };
 
 // Reduce-scatter over the warp: v[NV] per lane -> lane L holds the warp sums of
-// indices [L*NV/32, (L+1)*NV/32) in v[0 .. NV/32).
+// indices [L*NV/32, (L+1)*NV/32) in v[0 .. NV/32).  With NV = 16 the last
+// halving is replaced by a pairwise add: lane L then holds index L/2 (lanes L
+// and L^1 hold the same sum).
 template <int NV>
 __device__ __forceinline__ void warp_reduce_scatter(float (&v)[NV], int lane) {
+    static_assert(NV == 32 || NV == 16, "reduce-scatter of 16 or 32 values");
+    constexpr int ROUNDS = NV == 32 ? 5 : 4;
 #pragma unroll
-    for (int r = 0; r < 5; ++r) {
+    for (int r = 0; r < ROUNDS; ++r) {
         const int m = 16 >> r;
         const int half = NV >> (r + 1);
         const bool upper = (lane & m) != 0;
@@ -445,6 +451,7 @@ __device__ __forceinline__ void warp_reduce_scatter(float (&v)[NV], int lane) {
             v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
         }
     }
+    if constexpr (NV == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
 template <class C>
@@ -521,9 +528,10 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             constexpr int KCH = C::TWO ? C::KC : HL;
 #pragma unroll 1
             for (int ch = 0; ch < (C::TWO ? C::NCH : 1); ++ch) {
-                float e3[32];
+                constexpr int NE = KCH <= 16 ? 16 : 32;  // values reduce-scattered
+                float e3[NE];
 #pragma unroll
-                for (int k = 0; k < 32; ++k) e3[k] = 0.f;
+                for (int k = 0; k < NE; ++k) e3[k] = 0.f;
                 if (act) {
                     if constexpr (C::TWO) {
                         float* zrow = &R.zb[lane * A::ZS];
@@ -566,8 +574,12 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                         }
                     }
                 }
-                warp_reduce_scatter<32>(e3, lane);
-                if (lane < KCH) R.gW3[ch * KCH + lane] += e3[0];
+                warp_reduce_scatter<NE>(e3, lane);
+                if constexpr (NE == 16) {
+                    if (!(lane & 1) && (lane >> 1) < KCH) R.gW3[ch * KCH + (lane >> 1)] += e3[0];
+                } else {
+                    if (lane < KCH) R.gW3[ch * KCH + lane] += e3[0];
+                }
             }
             const float ob0 = ob[0];
             float b3 = ob0;

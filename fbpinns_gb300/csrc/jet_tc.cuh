@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
     for (int it = blockIdx.x; it < nit && !failed; it += gridDim.x) {
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
-        load_params<C>(S, net, j);
+        load_params<C, false>(S, net, j);
         // B_c[k][n] = W2[k][n] f_c[n], split hi/lo, rows k, K = n
         for (int i = tid; i < J * H2 * H1; i += blockDim.x) {
             const int c = i / (H2 * H1), r = i - c * (H2 * H1);

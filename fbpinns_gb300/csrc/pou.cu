@@ -321,42 +321,58 @@ struct PointPOU {
         for (int c = 0; c < J; ++c) U[c] = 0.f;
         const int e0 = (int)min((int64_t)pt_off[p], s_cap), e1 = (int)min((int64_t)pt_off[p + 1], s_cap);
         int cur = -1;
-        for (int e = e0; e <= e1; ++e) {
-            const int r = e < e1 ? p_take[e] : -2;
-            if (r != cur) {
-                if (cur >= 0) {
-                    quotient<XD, D2>(N, W, Ul);
+        // the pairs in groups of PU whose loads are issued together; the sums
+        // run in pair order as one pair at a time would
+        constexpr int PU = 4;
+        for (int eb = e0; eb <= e1; eb += PU) {
+            int rr[PU];
+            float rec[PU][RS];
 #pragma unroll
-                    for (int c = 0; c < J; ++c) U[c] += Ul[c];
-                    if (cur < u_cap) {
-                        float* so = slot_out + (size_t)cur * RS;
+            for (int q = 0; q < PU; ++q) {
+                const int e = eb + q;
+                rr[q] = e < e1 ? p_take[e] : -2;
+                if (e < e1) {
+                    const float4* po = reinterpret_cast<const float4*>(pair_out + (size_t)e * RS);
 #pragma unroll
-                        for (int c = 0; c < J; ++c) {
-                            so[c] = Ul[c];
-                            so[J + c] = W[c];
-                        }
+                    for (int h = 0; h < RS / 4; ++h) {
+                        const float4 v = po[h];
+                        rec[q][4 * h] = v.x;
+                        rec[q][4 * h + 1] = v.y;
+                        rec[q][4 * h + 2] = v.z;
+                        rec[q][4 * h + 3] = v.w;
                     }
                 }
-                if (r >= 0 && r < cur) atomicOr(status, FBP_STATUS_LEVEL_ORDER);
-                cur = r;
-#pragma unroll
-                for (int c = 0; c < J; ++c) N[c] = W[c] = 0.f;
             }
-            if (e < e1) {
-                const float4* po = reinterpret_cast<const float4*>(pair_out + (size_t)e * RS);
-                float rec[RS];
 #pragma unroll
-                for (int q = 0; q < RS / 4; ++q) {
-                    const float4 v = po[q];
-                    rec[4 * q] = v.x;
-                    rec[4 * q + 1] = v.y;
-                    rec[4 * q + 2] = v.z;
-                    rec[4 * q + 3] = v.w;
+            for (int q = 0; q < PU; ++q) {
+                const int e = eb + q;
+                if (e > e1) break;
+                const int r = rr[q];
+                if (r != cur) {
+                    if (cur >= 0) {
+                        quotient<XD, D2>(N, W, Ul);
+#pragma unroll
+                        for (int c = 0; c < J; ++c) U[c] += Ul[c];
+                        if (cur < u_cap) {
+                            float* so = slot_out + (size_t)cur * RS;
+#pragma unroll
+                            for (int c = 0; c < J; ++c) {
+                                so[c] = Ul[c];
+                                so[J + c] = W[c];
+                            }
+                        }
+                    }
+                    if (r >= 0 && r < cur) atomicOr(status, FBP_STATUS_LEVEL_ORDER);
+                    cur = r;
+#pragma unroll
+                    for (int c = 0; c < J; ++c) N[c] = W[c] = 0.f;
                 }
+                if (e < e1) {
 #pragma unroll
-                for (int c = 0; c < J; ++c) {
-                    N[c] += rec[c];
-                    W[c] += rec[J + c];
+                    for (int c = 0; c < J; ++c) {
+                        N[c] += rec[q][c];
+                        W[c] += rec[q][J + c];
+                    }
                 }
             }
         }

@@ -353,9 +353,16 @@ __global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t*
         for (int64_t j = threadIdx.x; j < m; j += blockDim.x) cnt[j] = 0;
         __syncthreads();
         const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
-        for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-            const int k = key[i];
-            if (k >= 0 && k < m) atomicAdd(&cnt[k], 1);
+        for (int64_t i0 = b0; i0 < b1; i0 += (int64_t)blockDim.x * 8) {  // loads first, then the counts
+            int kk[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int64_t i = i0 + (int64_t)u * blockDim.x + threadIdx.x;
+                kk[u] = i < b1 ? key[i] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (kk[u] >= 0 && kk[u] < m) atomicAdd(&cnt[kk[u]], 1);
         }
         __syncthreads();
         for (int64_t j = threadIdx.x; j < m; j += blockDim.x) hist[j * nchunks + ch] = cnt[j];
@@ -363,24 +370,63 @@ __global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t*
     }
 }
 
-constexpr int SCATTER_U = 4;  // 32-pair rows whose loads are issued together
+constexpr int SCATTER_U = 16;  // 32-pair rows whose loads are issued together
+constexpr int SCATTER_W = 4;  // warps per chunk (fewer when 4 bucket tables do not fit)
 
-// One warp per chunk of SORT_CH pairs (point-major).  A point's pairs have
-// distinct boxes, so each row of 32 pairs is placed point by point: the lanes
-// of one point read and advance distinct bucket counters, and the points of
-// the row follow each other in order -- a stable counting sort with no
-// intra-warp key matching.
-__global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
-                                    const int32_t* __restrict__ p_take, const int32_t* __restrict__ s_dev,
-                                    int64_t s_cap, int64_t m, int64_t nchunks,
-                                    const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
-    extern __shared__ int run[];  // per-bucket running offsets of this chunk
-    const int lane = threadIdx.x;  // blockDim.x == 32
+// One CTA of W <= SCATTER_W warps per chunk of SORT_CH pairs (point-major).
+// Each warp first counts the buckets of its part of the chunk; the running
+// offsets of warp w start at the chunk's bucket offset plus the counts of
+// warps < w, so the warps then place their quarters independently and the
+// result is the same stable order as one pass over the chunk.  A point's
+// pairs have distinct boxes, so each row of 32 pairs is placed point by
+// point: the lanes of one point read and advance distinct bucket counters,
+// and the points of the row follow each other in order (no key matching).
+__global__ void __launch_bounds__(SCATTER_W * 32)
+    sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
+                        const int32_t* __restrict__ p_take, const int32_t* __restrict__ s_dev, int64_t s_cap,
+                        int64_t m, int64_t nchunks, const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
+    extern __shared__ int run[];  // [W][m]: per-warp counts, then running offsets
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
+    int* myrun = run + (int64_t)w * m;
     const int64_t s = min((int64_t)*s_dev, s_cap);
+    const int64_t SUB = (SORT_CH + W - 1) / W;
     for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-        for (int64_t j = lane; j < m; j += 32) run[j] = hoff[j * nchunks + ch];
-        __syncwarp();
-        const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
+        for (int64_t j = threadIdx.x; j < m * W; j += blockDim.x) run[j] = 0;
+        __syncthreads();
+        const int64_t c0 = ch * SORT_CH, c1 = min(c0 + SORT_CH, s);
+        const int64_t b0 = min(c0 + (int64_t)w * SUB, c1), b1 = min(b0 + SUB, c1);
+        for (int64_t i0 = b0; i0 < b1; i0 += 32 * 8) {  // loads of 8 rows first, then the counts
+            int kk[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int64_t i = i0 + u * 32 + lane;
+                kk[u] = i < b1 ? key[i] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (kk[u] >= 0 && kk[u] < m) atomicAdd(&myrun[kk[u]], 1);
+        }
+        __syncthreads();
+        for (int64_t j0 = threadIdx.x; j0 < m; j0 += (int64_t)blockDim.x * 8) {
+            int oo[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int64_t j = j0 + (int64_t)u * blockDim.x;
+                oo[u] = j < m ? hoff[j * nchunks + ch] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int64_t j = j0 + (int64_t)u * blockDim.x;
+                if (j >= m) break;
+                int o = oo[u];
+                for (int v = 0; v < W; ++v) {
+                    const int c = run[(int64_t)v * m + j];
+                    run[(int64_t)v * m + j] = o;
+                    o += c;
+                }
+            }
+        }
+        __syncthreads();
         for (int64_t i0 = b0; i0 < b1; i0 += 32 * SCATTER_U) {
             int kk[SCATTER_U], nn[SCATTER_U], pp[SCATTER_U];
 #pragma unroll
@@ -406,8 +452,8 @@ __global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32
                     const int pt = __shfl_sync(0xffffffffu, nn[u], __ffs(todo) - 1);
                     const unsigned grp = __ballot_sync(0xffffffffu, (todo >> lane & 1u) && nn[u] == pt);
                     if ((grp >> lane & 1u) && ok) {
-                        const int o = run[k];
-                        run[k] = o + 1;
+                        const int o = myrun[k];
+                        myrun[k] = o + 1;
                         sd_rec[o] = make_int4((int32_t)i, pt, pp[u], 0);
                     }
                     todo &= ~grp;
@@ -415,7 +461,7 @@ __global__ void sort_scatter_kernel(const int32_t* __restrict__ key, const int32
                 }
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -603,10 +649,13 @@ extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, cons
     int32_t* hoff = hist + (hn + 1);
     int32_t* sums = hoff + (hn + 1);
     const size_t shm = (size_t)m * sizeof(int);
-    if (shm > 48 * 1024) {
+    int sw = SCATTER_W;  // warps per chunk in the scatter: one bucket table each
+    while (sw > 1 && shm * sw > 200 * 1024) sw >>= 1;
+    if (shm > 48 * 1024)
         FBP_CUDA_CHECK(cudaFuncSetAttribute(sort_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-        FBP_CUDA_CHECK(cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    }
+    if (shm * sw > 48 * 1024)
+        FBP_CUDA_CHECK(
+            cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(shm * sw)));
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 8);
         sort_hist_kernel<<<g, 256, shm, st>>>(m_take, s_dev, s_cap, m, nch, hist);
@@ -615,8 +664,8 @@ extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, cons
     int rc = scan_launch(hist, hoff, hn, sums, st);
     if (rc) return rc;
     if (nch > 0) {
-        const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32);
-        sort_scatter_kernel<<<g, 32, shm, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff,
+        const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32 / sw);
+        sort_scatter_kernel<<<g, 32 * sw, shm * sw, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff,
                                                  reinterpret_cast<int4*>(sd_rec));
         FBP_LAUNCH_CHECK();
         sort_starts_kernel<<<grid_for(m + 1, 256), 256, 0, st>>>(hoff, m, nch, sd_start);
