@@ -24,6 +24,8 @@ STATUS_BITS = {
 
 PROBLEM_NONE, PROBLEM_HO_HARDBC, PROBLEM_BURGERS, PROBLEM_POISSON2D, PROBLEM_WAVE_C, PROBLEM_HELMHOLTZ2D = range(6)
 D2_LAPLACIAN = 8  # FBP_D2_LAPLACIAN: one jet slot for the sum of the masked second derivatives
+ACT_TANH, ACT_SIN = 0, 1  # FBP_ACT_*: hidden-layer activation of the compiled networks
+ACTIVATIONS = {"tanh": ACT_TANH, "sin": ACT_SIN}
 
 
 class FBPLibraryError(RuntimeError):
@@ -38,7 +40,7 @@ class Boxes(C.Structure):
 
 class Net(C.Structure):
     _fields_ = [("xd", C.c_int32), ("h1", C.c_int32), ("h2", C.c_int32), ("ud", C.c_int32), ("d2mask", C.c_int32),
-                ("nparam", C.c_int32), ("theta", C.c_void_p), ("xmins", C.c_void_p), ("xmaxs", C.c_void_p),
+                ("nparam", C.c_int32), ("act", C.c_int32), ("theta", C.c_void_p), ("xmins", C.c_void_p), ("xmaxs", C.c_void_p),
                 ("flags", C.c_void_p), ("unnorms", C.c_void_p), ("m", C.c_int64)]
 
 
@@ -85,7 +87,7 @@ _SIG = {
                                      C.c_uint64, _P, _P]),
     "fbp_fma_probe": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_double), _P]),
     "fbp_tanh_probe": (C.c_int, [_P, _P, _I64, _P]),
-    "fbp_has_shape": (C.c_int, [_I32, _I32, _I32, _I32]),
+    "fbp_has_shape": (C.c_int, [_I32, _I32, _I32, _I32, _I32]),
 }
 
 _lib = None

@@ -49,11 +49,12 @@ def FBPINN_solution(c, all_params, active, x_batch):
     """The FBPINN at points x_batch with all subdomains (fbpinns/analysis.py:49-55), on the GPU engine."""
     from .engine import FBPINNEngine, inference_d2mask
     from .networks import pack_layers
-    from .trainers import FBPINNTrainer
+    from .trainers import FBPINNTrainer, NETWORK_ACTIVATIONS
     ap = _torch_tree(all_params)
     layers = ap["trainable"]["network"]["subdomain"]["layers"]
     sizes = [layers[0][0].shape[2]] + [w.shape[1] for w, _ in layers]
-    eng = FBPINNEngine(ap["static"]["decomposition"], sizes, inference_d2mask(sizes))
+    act = NETWORK_ACTIVATIONS.get(c.network, "tanh")
+    eng = FBPINNEngine(ap["static"]["decomposition"], sizes, inference_d2mask(sizes, act), activation=act)
     eng.set_theta(pack_layers([(torch.as_tensor(w), torch.as_tensor(b)) for w, b in layers]))
     dev = eng.device
     ap["static"]["problem"] = {k: (v.to(dev) if torch.is_tensor(v) else v) for k, v in ap["static"]["problem"].items()}

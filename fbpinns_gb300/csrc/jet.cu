@@ -5,6 +5,7 @@ namespace fbp {
 int jet_group_a(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 int jet_group_b(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 int jet_group_c(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
+int jet_group_d(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 
 static int check_net(const fbp_net* net, const fbp_pairs* pr) {
     FBP_REQUIRE(net && pr, FBP_ERR_INVALID, "jet: null descriptor");
@@ -28,7 +29,10 @@ static int dispatch(int mode, const fbp_net* net, const float* x, const fbp_pair
     if (r != 1) return r;
     r = jet_group_c(mode, net, x, pr, slot_out, out, grid, st);
     if (r != 1) return r;
-    set_error("jet: no compiled kernel for xd=%d h1=%d h2=%d d2mask=%d", net->xd, net->h1, net->h2, net->d2mask);
+    r = jet_group_d(mode, net, x, pr, slot_out, out, grid, st);
+    if (r != 1) return r;
+    set_error("jet: no compiled kernel for xd=%d h1=%d h2=%d d2mask=%d act=%d", net->xd, net->h1, net->h2,
+              net->d2mask, net->act);
     return FBP_ERR_UNSUPPORTED;
 }
 }  // namespace fbp
@@ -44,16 +48,18 @@ extern "C" int fbp_adjoint_pairs(const fbp_net* net, const float* x, const fbp_p
     return fbp::dispatch(1, net, x, pairs, slot_out, grad_part, grid, stream);
 }
 
-extern "C" int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask) {
+extern "C" int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act) {
     fbp_net net{};
     net.xd = xd;
     net.h1 = h1;
     net.h2 = h2;
     net.ud = 1;
     net.d2mask = d2mask;
+    net.act = act;
     fbp_pairs pr{};
     int r = fbp::jet_group_a(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     if (r == 1) r = fbp::jet_group_b(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     if (r == 1) r = fbp::jet_group_c(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
+    if (r == 1) r = fbp::jet_group_d(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     return r == FBP_OK ? 1 : 0;
 }

@@ -17,9 +17,49 @@
 
 namespace fbp {
 
-template <int XD_, int H1_, int H2_, int D2_>
+// Hidden-layer activations (fbp_net.act) and their jet rules.  Each keeps one
+// value per first-layer neuron in shared memory ("stored") from which the
+// value and the first two derivatives are recovered; zbar0 is the adjoint of
+// the jet map (a, a', a'') at z for the incoming sensitivities of a, a', a''.
+template <int ACT>
+struct Act;
+
+template <>
+struct Act<FBP_ACT_TANH> {  // FCN (fbpinns/networks.py:61-68): stored a = tanh z
+    __device__ __forceinline__ static float stored(float z) { return tanh_fast(z); }
+    __device__ __forceinline__ static void derivs(float s, float& a, float& d1, float& d2) {
+        a = s;
+        d1 = 1.0f - a * a;
+        d2 = -2.0f * a * d1;
+    }
+    __device__ __forceinline__ static void eval(float z, float& a, float& d1, float& d2) { derivs(tanh_fast(z), a, d1, d2); }
+    // third derivative of tanh: tanh' (6 a^2 - 2)
+    __device__ __forceinline__ static float zbar0(float ab, float d1b, float d2b, float a, float d1, float) {
+        return (ab + d1b * (-2.0f * a) + d2b * (6.0f * a * a - 2.0f)) * d1;
+    }
+};
+
+template <>
+struct Act<FBP_ACT_SIN> {  // SIREN (fbpinns/networks.py:102-131): stored z
+    __device__ __forceinline__ static float stored(float z) { return z; }
+    __device__ __forceinline__ static void derivs(float s, float& a, float& d1, float& d2) {
+        float sn, cs;
+        sincosf(s, &sn, &cs);
+        a = sn;
+        d1 = cs;
+        d2 = -sn;
+    }
+    __device__ __forceinline__ static void eval(float z, float& a, float& d1, float& d2) { derivs(z, a, d1, d2); }
+    // third derivative of sin: -cos
+    __device__ __forceinline__ static float zbar0(float ab, float d1b, float d2b, float, float d1, float d2) {
+        return ab * d1 + d1b * d2 - d2b * d1;
+    }
+};
+
+template <int XD_, int H1_, int H2_, int D2_, int ACT_ = FBP_ACT_TANH>
 struct Cfg {
-    static constexpr int XD = XD_, H1 = H1_, H2 = H2_, D2 = D2_;
+    static constexpr int XD = XD_, H1 = H1_, H2 = H2_, D2 = D2_, ACT = ACT_;
+    using AF = Act<ACT_>;
     static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
     static constexpr bool TWO = H2 > 0;
@@ -110,9 +150,9 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
 
 // Jet of one first-layer neuron's activation from a = tanh(z1).
 template <class C>
-__device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, float (&v)[C::J]) {
-    const float tp = 1.0f - a * a, tpp = -2.0f * a * tp;
-    v[0] = a;
+__device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, float (&v)[C::J]) {  // a: stored value
+    float tp, tpp;
+    C::AF::derivs(a, v[0], tp, tpp);
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) v[1 + d] = tp * S.cw[n * C::XD + d];
 #pragma unroll
@@ -123,9 +163,7 @@ __device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, floa
 template <class C>
 __device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J], float& a, float& tp,
                                          float& tpp) {
-    a = tanh_fast(z[0]);
-    tp = 1.0f - a * a;
-    tpp = -2.0f * a * tp;
+    C::AF::eval(z[0], a, tp, tpp);
     g[0] = a;
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) g[1 + d] = tp * z[1 + d];
@@ -162,8 +200,7 @@ __device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float a, fl
                 zb[1 + d] += g2 * z[1 + d];
             }
     }
-    const float ab = gb[0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f);
-    zb[0] = ab * tp;
+    zb[0] = C::AF::zbar0(gb[0], tpb, tppb, a, tp, tpp);
 }
 
 // Window jet (cosine window of fbpinns/windows.py:25-35 times flag plus 1-flag):
@@ -253,12 +290,13 @@ __device__ __forceinline__ void load_point(const SParams<C>& S, const float* __r
     for (int d = 0; d < C::XD; ++d) xn[d] = (x[(size_t)pt * C::XD + d] - S.mu[d]) * S.inv_sd[d];
 }
 
+// First-layer neuron n at the normalised point: the activation's stored value.
 template <class C>
 __device__ __forceinline__ float l1_act(const SParams<C>& S, const float (&xn)[C::XD], int n) {
     float z = S.b1[n];
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) z = fmaf(S.W1[n * C::XD + d], xn[d], z);
-    return tanh_fast(z);
+    return C::AF::stored(z);
 }
 
 // Layer-2 z-jets for neurons [k0, k0+KC) from first-layer activations a1row[n*stride]
@@ -635,8 +673,8 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                     for (int q = 0; q < NC; ++q) {
                         const int n = n0 + q;
-                        const float a = a1row[n];
-                        const float tp = 1.0f - a * a, tpp = -2.0f * a * tp;
+                        float a, tp, tpp;
+                        C::AF::derivs(a1row[n], a, tp, tpp);
                         float tpb = 0.f, tppb = 0.f, cwb[XD];
 #pragma unroll
                         for (int d = 0; d < XD; ++d) {
@@ -651,7 +689,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             for (int d = 0; d < XD; ++d)
                                 if ((C::slot_dims(s) >> d) & 1) cwb[d] += 2.0f * g * tpp * S.cw[n * XD + d];
                         }
-                        const float z1b = (vb[q][0] + tpb * (-2.0f * a) + tppb * (6.0f * a * a - 2.0f)) * tp;
+                        const float z1b = C::AF::zbar0(vb[q][0], tpb, tppb, a, tp, tpp);
 #pragma unroll
                         for (int d = 0; d < XD; ++d) r1[q * (XD + 1) + d] = fmaf(z1b, xn[d], cwb[d] * S.inv_sd[d]);
                         r1[q * (XD + 1) + XD] = z1b;
@@ -687,11 +725,11 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             float m[A::NB][3];
 #pragma unroll
                             for (int q = 0; q < A::NB; ++q) {
-                                const float a = R.a1[t * A::AS + n0 + q];
-                                const float tp = 1.0f - a * a;
+                                float a, tp, tpp;
+                                C::AF::derivs(R.a1[t * A::AS + n0 + q], a, tp, tpp);
                                 m[q][0] = a;
                                 m[q][1] = tp;
-                                m[q][2] = -2.0f * a * tp;
+                                m[q][2] = tpp;
                             }
                             const float* zr = &R.zb[t * A::ZS + k0];
 #pragma unroll

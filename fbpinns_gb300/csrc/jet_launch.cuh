@@ -15,10 +15,10 @@ int resident_grid(K kernel, int threads, size_t smem) {
     return per_sm * sm_count();
 }
 
-template <int XD, int H1, int H2, int D2>
+template <int XD, int H1, int H2, int D2, int ACT>
 int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, float* pair_out, int grid,
                    cudaStream_t st) {
-    using C = Cfg<XD, H1, H2, D2>;
+    using C = Cfg<XD, H1, H2, D2, ACT>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward: nparam %d != %d for this shape", net.nparam, C::P);
     static int auto_grid = 0;
     if (grid <= 0) {
@@ -30,10 +30,10 @@ int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, floa
     return FBP_OK;
 }
 
-template <int XD, int H1, int H2, int D2>
+template <int XD, int H1, int H2, int D2, int ACT>
 int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, const float* slot_out,
                    float* grad_part, int grid, cudaStream_t st) {
-    using C = Cfg<XD, H1, H2, D2>;
+    using C = Cfg<XD, H1, H2, D2, ACT>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "adjoint: nparam %d != %d for this shape", net.nparam, C::P);
     const size_t shm = sizeof(WarpRows<C>) * AdjW<C>::W;
     static bool attr_set = false;
@@ -52,19 +52,20 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
 }
 
 // Tries one shape; returns 1 (not this shape) or the launch status.
-template <int XD, int H1, int H2, int D2>
+template <int XD, int H1, int H2, int D2, int ACT>
 int try_shape(int mode, const fbp_net& net, const float* x, const fbp_pairs& pr, const float* slot_out, float* out,
               int grid, cudaStream_t st) {
-    if (net.xd != XD || net.h1 != H1 || net.h2 != H2 || net.d2mask != D2) return 1;
+    if (net.xd != XD || net.h1 != H1 || net.h2 != H2 || net.d2mask != D2 || net.act != ACT) return 1;
     if (mode == 2) return FBP_OK;  // shape query: compiled
-    if (mode == 0) return launch_forward<XD, H1, H2, D2>(net, x, pr, out, grid, st);
-    return launch_adjoint<XD, H1, H2, D2>(net, x, pr, slot_out, out, grid, st);
+    if (mode == 0) return launch_forward<XD, H1, H2, D2, ACT>(net, x, pr, out, grid, st);
+    return launch_adjoint<XD, H1, H2, D2, ACT>(net, x, pr, slot_out, out, grid, st);
 }
 
 }  // namespace fbp
 
-#define FBP_TRY(XD, H1, H2, D2)                                                            \
-    {                                                                                      \
-        int r_ = fbp::try_shape<XD, H1, H2, D2>(mode, *net, x, *pr, slot_out, out, grid, st); \
-        if (r_ != 1) return r_;                                                            \
+#define FBP_TRY_ACT(XD, H1, H2, D2, ACT)                                                         \
+    {                                                                                            \
+        int r_ = fbp::try_shape<XD, H1, H2, D2, ACT>(mode, *net, x, *pr, slot_out, out, grid, st); \
+        if (r_ != 1) return r_;                                                                  \
     }
+#define FBP_TRY(XD, H1, H2, D2) FBP_TRY_ACT(XD, H1, H2, D2, FBP_ACT_TANH)

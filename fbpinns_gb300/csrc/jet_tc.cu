@@ -49,6 +49,8 @@ extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fb
                 "fbp_forward_pairs_tc: null network pointer");
     FBP_REQUIRE(pairs->sd_rec && pairs->items && pairs->n_items, FBP_ERR_INVALID,
                 "fbp_forward_pairs_tc: null pair pointer");
+    FBP_REQUIRE(net->act == FBP_ACT_TANH, FBP_ERR_UNSUPPORTED,
+                "fbp_forward_pairs_tc: only tanh networks are compiled (act=%d)", net->act);
     FBP_REQUIRE(net->ud == 1 && net->h1 == 16 && net->h2 == 16, FBP_ERR_UNSUPPORTED,
                 "fbp_forward_pairs_tc: only the xd-16-16-1 networks are compiled (got h1=%d h2=%d ud=%d)", net->h1,
                 net->h2, net->ud);

@@ -207,11 +207,11 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
                 float av[NA][4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const float a = l1_act<C>(S, xn, n4 + q);
-                    const float tp = 1.0f - a * a;
+                    float a, tp, tpp;
+                    C::AF::derivs(l1_act<C>(S, xn, n4 + q), a, tp, tpp);
                     av[0][q] = a;
                     av[1][q] = tp;
-                    if constexpr (NA > 2) av[NA - 1][q] = -2.0f * a * tp;
+                    if constexpr (NA > 2) av[NA - 1][q] = tpp;
                 }
                 const uint32_t off = kmajor16_off(tid, n4) >> 2;
 #pragma unroll

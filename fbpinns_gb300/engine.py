@@ -212,7 +212,8 @@ def tc_supported(xd, h1, h2):
 class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
-    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None, tensor_cores=None):
+    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None, tensor_cores=None,
+                 activation="tanh"):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -231,18 +232,25 @@ class FBPINNEngine:
         self.h2 = ls[2] if len(ls) == 4 else 0
         self.P = fcn_param_count(ls)
         self.d2mask = int(d2mask)
-        if not _lib.load().fbp_has_shape(self.xd, self.h1, self.h2, self.d2mask):
+        if activation not in _lib.ACTIVATIONS:
+            raise ValueError(f"activation must be one of {sorted(_lib.ACTIVATIONS)}, not {activation!r}")
+        self.activation = activation
+        self.act = _lib.ACTIVATIONS[activation]
+        if not _lib.load().fbp_has_shape(self.xd, self.h1, self.h2, self.d2mask, self.act):
             raise _lib.FBPLibraryError(
-                f"no compiled jet kernels for layer sizes {ls} with second derivatives along dims "
-                f"{[d for d in range(self.xd) if (self.d2mask >> d) & 1]}; add the shape to csrc/jet_inst_*.cu")
+                f"no compiled jet kernels for layer sizes {ls} ({activation}) with second derivatives along dims "
+                f"{[d for d in range(self.xd) if (self.d2mask >> d) & 1]}"
+                f"{' (Laplacian slot)' if self.d2mask & _lib.D2_LAPLACIAN else ''}; "
+                f"add the shape to csrc/jet_inst_*.cu")
         self.J = jet_size(self.xd, self.d2mask)
         self.chunk = int(chunk)
         self.launch_grid = int(grid) if grid else 0
         # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
         # None = wherever available, True = required, False = CUDA-core FMA kernel
-        tc_ok = tc_supported(self.xd, self.h1, self.h2)
+        tc_ok = tc_supported(self.xd, self.h1, self.h2) and self.act == _lib.ACT_TANH
         if tensor_cores and not tc_ok:
-            raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} (compiled: 2-16-16-1)")
+            raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} ({activation}); "
+                                       f"compiled: 2-16-16-1 tanh")
         self.tensor_cores = tc_ok if tensor_cores is None else bool(tensor_cores)
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
@@ -271,6 +279,7 @@ class FBPINNEngine:
         n.xd, n.h1, n.h2, n.ud = self.xd, self.h1, self.h2, 1
         n.d2mask = self.d2mask if d2mask is None else d2mask
         n.nparam = self.P
+        n.act = self.act
         n.theta = _lib.ptr(self.theta if theta is None else theta)
         n.xmins, n.xmaxs, n.flags, n.unnorms = _lib.ptr(g.xmins), _lib.ptr(g.xmaxs), _lib.ptr(g.flags), _lib.ptr(g.unnorms)
         n.m = self.m
@@ -454,13 +463,14 @@ def constrained_jets(cfn, all_params, x, U, xd, d2mask):
     return torch.cat(out, dim=1)
 
 
-def inference_d2mask(layer_sizes):
+def inference_d2mask(layer_sizes, activation="tanh"):
     """A compiled jet mask for value-only evaluation of this network shape."""
     lib = _lib.load()
     xd = layer_sizes[0]
     h1 = layer_sizes[1]
     h2 = layer_sizes[2] if len(layer_sizes) == 4 else 0
-    for mask in range(1 << xd):
-        if lib.fbp_has_shape(xd, h1, h2, mask):
+    act = _lib.ACTIVATIONS[activation]
+    for mask in list(range(1 << xd)) + [m | _lib.D2_LAPLACIAN for m in range(1, 1 << xd)]:
+        if lib.fbp_has_shape(xd, h1, h2, mask, act):
             return mask
-    raise _lib.FBPLibraryError(f"no compiled jet kernels for layer sizes {list(layer_sizes)}")
+    raise _lib.FBPLibraryError(f"no compiled jet kernels for layer sizes {list(layer_sizes)} ({activation})")

@@ -58,8 +58,9 @@ class PlainStep:
         rows = theta[ids]
         layers = unpack_layers(rows, eng.layer_sizes)
         h = xn
+        act = torch.sin if eng.activation == "sin" else torch.tanh
         for w, b in layers[:-1]:
-            h = torch.tanh(torch.baddbmm(b[:, None, :], h, w.transpose(1, 2)))
+            h = act(torch.baddbmm(b[:, None, :], h, w.transpose(1, 2)))
         w, b = layers[-1]
         u = torch.baddbmm(b[:, None, :], h, w.transpose(1, 2))
         un = g.unnorms[ids]

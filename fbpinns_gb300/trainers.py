@@ -24,7 +24,10 @@ import torch
 
 from . import _lib
 from .engine import FBPINNEngine, FBPINNJet, constrained_jets, d2mask_of, jet_index
-from .networks import fcn_param_count, pack_layers, unpack_layers, FCN
+from .networks import fcn_param_count, pack_layers, unpack_layers, FCN, SIREN
+
+# network classes with compiled jet kernels, by hidden-layer activation
+NETWORK_ACTIVATIONS = {FCN: "tanh", SIREN: "sin"}
 from .optim import adam_update
 from .takes import get_inputs, split_takes, inside_models, grid_of  # noqa: F401  (re-exported API)
 
@@ -249,8 +252,9 @@ class FBPINNTrainer:
         m, xd = st_dec["m"], st_dec["xd"]
         assert all_params["static"]["domain"]["xd"] == all_params["static"]["problem"]["dims"][1] == xd
         logger.info(f"Total number of subdomains: {m}")
-        if c.network is not FCN:
-            raise NotImplementedError("the compiled jet kernels implement the FCN network")
+        if c.network not in NETWORK_ACTIVATIONS:
+            raise NotImplementedError("the compiled jet kernels implement the FCN and SIREN networks")
+        activation = NETWORK_ACTIVATIONS[c.network]
         net_static, net_tr = init_subdomain_networks(c.network, c.network_init_kwargs, m, c.seed)
         layer_sizes = list(c.network_init_kwargs["layer_sizes"])
         scheduler = c.scheduler(all_params=all_params, n_steps=c.n_steps, **c.scheduler_kwargs)
@@ -267,10 +271,11 @@ class FBPINNTrainer:
         single = len(constraints_global) == 1 and not all_params["trainable"].get("problem")
         use_fused = spec is not None and single
         if use_fused and spec.get("laplacian") and d2 and _lib.load().fbp_has_shape(
-                xd, layer_sizes[1], layer_sizes[2] if len(layer_sizes) == 4 else 0, d2 | _lib.D2_LAPLACIAN):
+                xd, layer_sizes[1], layer_sizes[2] if len(layer_sizes) == 4 else 0, d2 | _lib.D2_LAPLACIAN,
+                _lib.ACTIVATIONS[activation]):
             d2 |= _lib.D2_LAPLACIAN  # the residual needs only the Laplacian: one jet slot for it
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
-                           tensor_cores=getattr(c, "tensor_cores", None))
+                           tensor_cores=getattr(c, "tensor_cores", None), activation=activation)
         eng.set_theta(pack_layers(net_tr["layers"]))
         for k, v in list(all_params["trainable"].get("problem", {}).items()):
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()

@@ -54,6 +54,10 @@ extern "C" {
  * (Poisson, Helmholtz); the jet then has 1 + xd + 1 components. */
 #define FBP_D2_LAPLACIAN 8
 
+/* Hidden-layer activations of the compiled networks (fbp_net.act). */
+#define FBP_ACT_TANH 0   /* FCN (fbpinns/networks.py:61-68) */
+#define FBP_ACT_SIN 1    /* SIREN (fbpinns/networks.py:102-131) */
+
 /* Device status word bits (written by kernels into an int32 the caller owns). */
 #define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */
 #define FBP_STATUS_SLOT_OVERFLOW 2      /* more (point, level) slots than capacity */
@@ -99,9 +103,10 @@ typedef struct fbp_net {
     int32_t ud;           /* output dimension, must be 1 */
     int32_t d2mask;       /* dims with a pure second-derivative jet */
     int32_t nparam;       /* P: parameters per subdomain (packed layout below) */
+    int32_t act;          /* hidden-layer activation, FBP_ACT_* */
     /* theta (m, P): for each layer in order, W (fan_out, fan_in) row-major
-     * then b (fan_out) — the reference's FCN (w, b) list flattened
-     * (fbpinns/networks.py:43-68). */
+     * then b (fan_out) — the reference's FCN / SIREN (w, b) list flattened
+     * (fbpinns/networks.py:43-68, 102-131). */
     const float* theta;
     const float* xmins;   /* (m, xd) subdomain boxes (norm + window) */
     const float* xmaxs;   /* (m, xd) */
@@ -252,9 +257,10 @@ int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs
 int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pairs,
                          float* pair_out, int32_t* status, int32_t grid, void* stream);
 
-/* 1 if the per-pair jet kernels are compiled for this network shape and jet
- * mask (ud = 1), else 0.  Lets a caller fail early with a clear message. */
-int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask);
+/* 1 if the per-pair jet kernels are compiled for this network shape, jet
+ * mask and activation (FBP_ACT_*; ud = 1), else 0.  Lets a caller fail early
+ * with a clear message. */
+int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act);
 
 /* POU combination per point (the two segment sums and the divide of
  * fbpinns/trainers.py:162-170, on jets by the quotient rule):

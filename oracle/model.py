@@ -102,11 +102,13 @@ def cosine_window(xmin, xmax, x):
     return torch.prod(ws, dim=1, keepdim=True)
 
 
-def fcn(layers, x):
-    """``fbpinns/networks.py:61-68`` batched over pairs: W (s,fo,fi), b (s,fo)."""
+def fcn(layers, x, activation="tanh"):
+    """``fbpinns/networks.py:61-68`` (FCN, tanh) and ``:102-131`` (SIREN, sin),
+    batched over pairs: W (s,fo,fi), b (s,fo)."""
+    act = {"tanh": torch.tanh, "sin": torch.sin}[activation]
     for w, b in layers[:-1]:
         x = torch.einsum("sij,sj->si", w, x) + b
-        x = torch.tanh(x)
+        x = act(x)
     w, b = layers[-1]
     return torch.einsum("sij,sj->si", w, x) + b
 
@@ -134,7 +136,7 @@ def fbpinn_model(P, x_batch, takes, constraining_fn):
     x_norm = norm((xmax + xmin) / 2, (xmax - xmin) / 2, x_take)
     # network_fn  (networks.py:61-68)
     layers = [(w[m_take], b[m_take]) for w, b in P["layers"]]
-    u_raw = fcn(layers, x_norm)
+    u_raw = fcn(layers, x_norm, P.get("activation", "tanh"))
     # unnorm_fn  (decompositions.py:191-194)
     un = P["unnorms"][m_take]
     u = unnorm(un[:, 0:1], un[:, 1:2], u_raw)

@@ -29,8 +29,11 @@ sys.path.insert(0, HERE)
 import jaxshim  # noqa: E402
 
 
+OUT = HERE
+
+
 def save(name, **arrays):
-    path = os.path.join(HERE, name)
+    path = os.path.join(OUT, name)
     np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
     print(f"wrote {name}: " + ", ".join(f"{k}{np.asarray(v).shape}" for k, v in arrays.items()))
 
@@ -38,7 +41,10 @@ def save(name, **arrays):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--out", default=HERE, help="output folder (default: next to this script)")
     args = ap.parse_args()
+    global OUT
+    OUT = args.out
     jaxshim.install()
     sys.path.insert(0, args.ref)
     from fbpinns import decompositions_base, decompositions, windows, networks, schedulers
@@ -204,13 +210,13 @@ def main():
         dmax = np.min(np.abs(xb[:, None, :] - xmaxs[None]), axis=(1, 2))
         return (dmin > margin) & (dmax > margin)
 
-    def model_case(tag, decomp, sp_params, problem, pkw, layer_sizes, xb, seed, dims):
+    def model_case(tag, decomp, sp_params, problem, pkw, layer_sizes, xb, seed, dims, network="FCN", wscale=1.0):
         r = np.random.default_rng(seed)
         ps_prob = problem.init_params(**pkw)[0]
         m = sp_params["m"]
         layers = []
         for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
-            v = np.sqrt(1 / fi)
+            v = wscale * np.sqrt(1 / fi)
             layers.append((jnp.array(r.uniform(-v, v, (m, fo, fi))), jnp.array(r.uniform(-v, v, (m, fo)))))
         sub = sp_params["subdomain"]["params"]
         keep = far_from_edges(xb, np.asarray(sub[0]), np.asarray(sub[1]), 1e-2)
@@ -220,7 +226,8 @@ def main():
         active = np.ones(m, dtype=int)
         takes, all_ims, (_, _, _, cut_all, _) = trainers.get_inputs(jnp.array(xb), active, all_params, decomp)
         apc = {"static": cut_all(all_params["static"]), "trainable": cut_all(all_params["trainable"])}
-        mf = (decomp.norm_fn, networks.FCN.network_fn, decomp.unnorm_fn, decomp.window_fn, problem.constraining_fn)
+        mf = (decomp.norm_fn, getattr(networks, network).network_fn, decomp.unnorm_fn, decomp.window_fn,
+              problem.constraining_fn)
         u, wp, us, ws, ur = trainers.FBPINN_model(apc, jnp.array(xb), takes, mf, verbose=False)
         # POU-combined u before the constraining operator
         mf_id = mf[:4] + (lambda a, xb_, u_: u_,)
@@ -263,6 +270,15 @@ def main():
     loss_fns["multilevel"] = lambda ap_, xb, u, j: np.mean((j[(0, 0)] + j[(1, 1)]) ** 2)
     xml = rng.uniform(0, 1, (600, 2))
     model_case("multilevel", DM, spm, BU, dict(), [2, 8, 8, 1], xml, 14, [0, 1])
+    # SIREN networks (networks.py:102-131, U(+-sqrt(6/fan_in)) weights); own
+    # generator so the draws above are unchanged
+    rng_s = np.random.default_rng(31)
+    loss_fns["ho_hardbc_siren"] = loss_fns["ho_hardbc"]
+    model_case("ho_hardbc_siren", D, sp, HOH, dict(d=2, w0=80, sd=0.1), [1, 8, 8, 1], xho, 15, [0],
+               network="SIREN", wscale=np.sqrt(6.0))
+    loss_fns["multilevel_siren"] = loss_fns["multilevel"]
+    model_case("multilevel_siren", DM, spm, BU, dict(), [2, 8, 8, 1], rng_s.uniform(0, 1, (600, 2)), 16, [0, 1],
+               network="SIREN", wscale=np.sqrt(6.0))
 
     # constraining functions and losses on given jets
     xc = rng.uniform([-1, -1, 0], [1, 1, 1], (64, 3))

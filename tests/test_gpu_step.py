@@ -28,21 +28,22 @@ JET_TOL = 1e-5
 GRAD_TOL = 1e-4
 
 
-def _engine(static, layers, d2mask, chunk=64):
-    eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk)
+def _engine(static, layers, d2mask, chunk=64, activation="tanh"):
+    eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk, activation=activation)
     eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
     return eng
 
 
 @pytest.mark.parametrize("tag,dims,d2", [("ho_hardbc", [0], 1), ("burgers", [0, 1], 1), ("wave", [0, 1, 2], 7),
-                                         ("multilevel", [0, 1], 3)])
+                                         ("multilevel", [0, 1], 3), ("ho_hardbc_siren", [0], 1),
+                                         ("multilevel_siren", [0, 1], 3)])
 def test_jets_vs_reference_golden(cuda, tag, dims, d2):
     """POU-combined network jets (before the constraint) vs the reference's
-    forward values and their float64 finite differences."""
+    forward values and their float64 finite differences (FCN and SIREN)."""
     g = golden(f"model_{tag}.npz")
-    static = decomposition(tag)
+    static = decomposition(tag.replace("_siren", ""))
     layers = golden_layers(g)
-    eng = _engine(static, layers, d2)
+    eng = _engine(static, layers, d2, activation="sin" if tag.endswith("_siren") else "tanh")
     ps = eng.points(torch.tensor(g["x_batch"], dtype=torch.float32))
     U = FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy()
     xd = len(static["subdomain"]["params"][0][0])
@@ -128,6 +129,38 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
     inactive = np.setdiff1d(np.arange(static["m"]), a_ims)
     assert np.all(grad[inactive] == 0)
+
+
+@pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("poisson", False), ("poisson", True)])
+def test_siren_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
+    """SIREN networks (sin activations, U(+-sqrt(6/fan_in)) weights): fused loss
+    and per-subdomain gradients vs the float64 oracle."""
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    ls = [ls[0], 8, 8, 1]
+    static = decomposition(recipe)
+    layers64 = [(w * math.sqrt(6.0), b * math.sqrt(6.0)) for w, b in random_layers(ls, static["m"], seed=7)]
+    layers32 = [(w.float().double(), b.float().double()) for w, b in layers64]
+    x = _points(recipe if recipe != "multilevel" else "poisson", 500, 23)
+    prob_static = pcls.init_params(**pkw)[0]
+    P = oracle_params(static, layers32, opar)
+    P["activation"] = "sin"
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(static["m"], dtype=int), p[0].numpy(),
+                                                          p[1].numpy(), static["subdomain"]["pou"].numpy())
+    loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
+                                           [OM.get_jmaps(_required(name))], ocls)
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
+    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0), activation="sin")
+    assert not eng.tensor_cores
+    eng.set_state(active)
+    eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+    ps = eng.points(torch.tensor(x))
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
+    assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
 
 
 def test_laplacian_jets_match_sum_of_second_derivatives(cuda):

@@ -77,3 +77,17 @@ def test_model_save_and_load(cuda, tmp_path, monkeypatch):
     u_loaded = FBPINN_solution(c2, all_params, active, x)
     u_live = FBPINNTrainer.predict(tr.engine, tr.all_params, c.problem, x)
     assert torch.allclose(u_loaded, u_live, rtol=1e-6, atol=1e-6)
+
+
+def test_siren_network_trains_fused(cuda):
+    """A SIREN network (sin activations, networks.py:102-131) through the fused
+    engine: the HO problem trains and the saved-model inference agrees."""
+    from fbpinns_gb300.networks import SIREN
+    c = configs.ho(n_steps=150)
+    c.network = SIREN
+    c.summary_freq, c.test_freq = 50, 150
+    tr = FBPINNTrainer(c)
+    tr.train()
+    assert tr.engine.activation == "sin" and not tr.engine.tensor_cores
+    losses = [h["loss"] for h in tr.history]
+    assert all(math.isfinite(v) for v in losses) and losses[-1] < losses[0]

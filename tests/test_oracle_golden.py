@@ -95,10 +95,11 @@ def test_level_params_match_reference(name, recipe):
 
 
 def _oracle_params(g, tag, decomp):
-    ps_full = _level_full(tag)
+    ps_full = _level_full(tag.replace("_siren", ""))
     P = {"xmins": torch.tensor(ps_full[0]), "xmaxs": torch.tensor(ps_full[1]),
          "flags": torch.tensor(ps_full[4]), "unnorms": torch.tensor(ps_full[5]),
-         "pou": torch.tensor(ps_full[6]), "layers": []}
+         "pou": torch.tensor(ps_full[6]), "layers": [],
+         "activation": "sin" if tag.endswith("_siren") else "tanh"}
     i = 0
     while f"W{i}" in g:
         P["layers"].append((torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])))
@@ -130,9 +131,11 @@ PROBLEMS = {
              [0, 1, 2]),
     "multilevel": (OP.BurgersEquation2D, {"sd": 0.1, "nu": 0.01 / np.pi}, [0, 1]),
 }
+PROBLEMS["ho_hardbc_siren"] = PROBLEMS["ho_hardbc"]  # SIREN networks (networks.py:102-131)
+PROBLEMS["multilevel_siren"] = PROBLEMS["multilevel"]
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel", "ho_hardbc_siren", "multilevel_siren"])
 def test_model_forward_matches_reference(tag):
     """oracle FBPINN_model (float64) == the reference's FBPINN_model run on numpy."""
     g = golden(f"model_{tag}.npz")
@@ -150,7 +153,7 @@ def test_model_forward_matches_reference(tag):
     np.testing.assert_allclose(ur.numpy(), g["us_raw"], rtol=1e-10, atol=1e-12)
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel", "ho_hardbc_siren", "multilevel_siren"])
 def test_model_jets_match_reference_fd(tag):
     """oracle nested-jvp jets == float64 finite differences of the reference model."""
     g = golden(f"model_{tag}.npz")
@@ -169,7 +172,7 @@ def test_model_jets_match_reference_fd(tag):
             assert err < 2e-6, (nm, err)
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "ho_hardbc_siren"])
 def test_loss_matches_reference(tag):
     g = golden(f"model_{tag}.npz")
     prob, pp, dims = PROBLEMS[tag]
@@ -177,7 +180,7 @@ def test_loss_matches_reference(tag):
     P["problem"] = pp
     takes = (g["m_take"], g["n_take"], g["p_take"], g["np_take"], int(g["npou"]))
     x = torch.tensor(g["x_batch"])
-    req = {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))),
+    req = {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))), "ho_hardbc_siren": ((0, ()), (0, (0,)), (0, (0, 0))),
            "burgers": ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0))),
            "wave": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2)))}[tag]
     loss = OM.fbpinn_loss(P, [[x]], [takes], [OM.get_jmaps(req)], prob)
