@@ -349,9 +349,14 @@ def run_fused(args, world, rank, local):
         best = max(best, flops.value / (a.elapsed_time(b) * 1e-3) / 1e12)
     dom = max(("forward_pairs", "adjoint_pairs"), key=lambda k: timings[k])
     ach = (fl_adj if dom == "adjoint_pairs" else fl_fwd) / (timings[dom] * 1e-3) / 1e12
+    # DRAM traffic of the adjoint per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
+    # adjoint_pairs_kernel<Cfg<2,16,16,11>> in one capture of this workload at 2^16 points
+    # (52.58 MB + 0.41 MB for about 2.34e6 pairs), scaled by this run's pairs (traffic grows with the pairs)
+    traffic = (52.579328e6 + 0.405504e6) / 2.3426e6 * pairs if (dom == "adjoint_pairs" and J == 4) else None
     roofline = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": best, "unit": "TFLOP/s", "frac": ach / best,
                 "peak_source": "FP32 FMA probe (fbp_fma_probe) measured in this run; MEASURED_PEAKS.json has no FP32 figure",
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": "ncu DRAM bytes of the adjoint at 2^16 points scaled by pairs" if traffic else None,
                 "kernel_ms": {k: round(v, 4) for k, v in timings.items()},
                 "algorithmic_flops_per_launch": {"forward_pairs": fl_fwd, "adjoint_pairs": fl_adj}}
 
