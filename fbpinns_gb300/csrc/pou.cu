@@ -443,69 +443,225 @@ __device__ __forceinline__ double block_sum_double(double v, double* sh) {
     return r;
 }
 
+// Constraint, residual and seeds of one point from its unconstrained jets u:
+// returns r^2 and leaves the seed dL/dU (before the 1/npou of the POU sum) in ub.
 template <int XD, int D2>
-__global__ void __launch_bounds__(POU_T) pou_loss_kernel(fbp_problem P, int64_t n, int npou, float inv_n,
-                                                          const float* __restrict__ x,
-                                                          const int32_t* __restrict__ pt_off,
-                                                          const int32_t* __restrict__ np_off,
-                                                          const int32_t* __restrict__ p_take,
-                                                          const float* __restrict__ pair_out,
-                                                          float* __restrict__ slot_out, float* __restrict__ U_out,
-                                                          int64_t s_cap, int64_t u_cap,
-                                                          double* __restrict__ loss_part, int32_t* status) {
+__device__ __forceinline__ float point_residual(const fbp_problem& P, float inv_n, const float* __restrict__ x,
+                                                int64_t p, const float (&u)[JL<XD, D2>::J],
+                                                float* __restrict__ U_out, float (&ub)[JL<XD, D2>::J]) {
     constexpr int J = JL<XD, D2>::J;
-    __shared__ double sh[POU_T / 32];
-    double acc = 0.0;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        float u[J];
-        PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, s_cap, u_cap, status);
-        float xp[XD];
+    float xp[XD];
 #pragma unroll
-        for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
-        float A[J], B[J];
-        ansatz<XD, D2>(P, xp, A, B);
-        float uc[J];
-        uc[0] = A[0] + B[0] * u[0];
+    for (int d = 0; d < XD; ++d) xp[d] = x[p * XD + d];
+    float A[J], B[J];
+    ansatz<XD, D2>(P, xp, A, B);
+    float uc[J];
+    uc[0] = A[0] + B[0] * u[0];
 #pragma unroll
-        for (int d = 0; d < XD; ++d) uc[1 + d] = A[1 + d] + B[1 + d] * u[0] + B[0] * u[1 + d];
+    for (int d = 0; d < XD; ++d) uc[1 + d] = A[1 + d] + B[1 + d] * u[0] + B[0] * u[1 + d];
 #pragma unroll
-        for (int s = 0; s < JL<XD, D2>::NS; ++s) {
-            float v = A[1 + XD + s] + B[1 + XD + s] * u[0] + B[0] * u[1 + XD + s];
+    for (int s = 0; s < JL<XD, D2>::NS; ++s) {
+        float v = A[1 + XD + s] + B[1 + XD + s] * u[0] + B[0] * u[1 + XD + s];
 #pragma unroll
-            for (int d = 0; d < XD; ++d)
-                if ((JL<XD, D2>::slot_dims(s) >> d) & 1) v += 2.0f * B[1 + d] * u[1 + d];
-            uc[1 + XD + s] = v;
-        }
-        if (U_out) {
-#pragma unroll
-            for (int c = 0; c < J; ++c) U_out[p * J + c] = uc[c];
-        }
-        float dr[J];
-        const float r = residual<XD, D2>(P, xp, uc, dr);
-        acc += (double)r * (double)r;
-        // seeds: dL/duc = (2 r / n) dr/duc, then the ansatz adjoint
-        const float g = 2.0f * r * inv_n;
-        float ucb[J], ub[J];
-#pragma unroll
-        for (int c = 0; c < J; ++c) ucb[c] = g * dr[c];
-        ub[0] = B[0] * ucb[0];
-#pragma unroll
-        for (int d = 0; d < XD; ++d) {
-            ub[0] += B[1 + d] * ucb[1 + d];
-            ub[1 + d] = B[0] * ucb[1 + d];
-        }
-#pragma unroll
-        for (int s = 0; s < JL<XD, D2>::NS; ++s) {
-            ub[0] += B[1 + XD + s] * ucb[1 + XD + s];
-#pragma unroll
-            for (int d = 0; d < XD; ++d)
-                if ((JL<XD, D2>::slot_dims(s) >> d) & 1) ub[1 + d] += 2.0f * B[1 + d] * ucb[1 + XD + s];
-            ub[1 + XD + s] = B[0] * ucb[1 + XD + s];
-        }
-        PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out, u_cap);
+        for (int d = 0; d < XD; ++d)
+            if ((JL<XD, D2>::slot_dims(s) >> d) & 1) v += 2.0f * B[1 + d] * u[1 + d];
+        uc[1 + XD + s] = v;
     }
-    const double tot = block_sum_double(acc, sh);
-    if (threadIdx.x == 0) loss_part[blockIdx.x] = tot;
+    if (U_out) {
+#pragma unroll
+        for (int c = 0; c < J; ++c) U_out[p * J + c] = uc[c];
+    }
+    float dr[J];
+    const float r = residual<XD, D2>(P, xp, uc, dr);
+    // seeds: dL/duc = (2 r / n) dr/duc, then the ansatz adjoint
+    const float g = 2.0f * r * inv_n;
+    float ucb[J];
+#pragma unroll
+    for (int c = 0; c < J; ++c) ucb[c] = g * dr[c];
+    ub[0] = B[0] * ucb[0];
+#pragma unroll
+    for (int d = 0; d < XD; ++d) {
+        ub[0] += B[1 + d] * ucb[1 + d];
+        ub[1 + d] = B[0] * ucb[1 + d];
+    }
+#pragma unroll
+    for (int s = 0; s < JL<XD, D2>::NS; ++s) {
+        ub[0] += B[1 + XD + s] * ucb[1 + XD + s];
+#pragma unroll
+        for (int d = 0; d < XD; ++d)
+            if ((JL<XD, D2>::slot_dims(s) >> d) & 1) ub[1 + d] += 2.0f * B[1 + d] * ucb[1 + XD + s];
+        ub[1 + XD + s] = B[0] * ucb[1 + XD + s];
+    }
+    return r * r;
+}
+
+// Fused POU + constraint + residual + loss + seeds, one warp per 32
+// consecutive points.  Their pairs are one contiguous range of pair_out whose
+// slot ids (p_take) ascend, so the warp reads the range row by row (32 pairs,
+// coalesced), sums each row's records per slot with a segmented shuffle scan
+// and adds the row sums into a per-warp shared-memory table of the range's
+// slots (rows in order: a fixed summation order).  Then per slot the quotient
+// jets, per point (lane) the constraint, residual and seeds, per slot the
+// seeds dL/dN, and the slot records [dL/dN | W] leave coalesced.  A warp whose
+// slots do not fit the table runs the same steps one point per lane.
+constexpr int POU_WARPS = 4;
+
+// slots per warp in the shared-memory table: up to 256, within 40 KB per CTA
+__host__ __device__ constexpr int pou_slotcap(int rs) {
+    return 40960 / (POU_WARPS * rs * 4) < 256 ? 40960 / (POU_WARPS * rs * 4) : 256;
+}
+
+template <int XD, int D2>
+__global__ void __launch_bounds__(POU_WARPS * 32) pou_loss_kernel(fbp_problem P, int64_t n, int npou, float inv_n,
+                                                                   const float* __restrict__ x,
+                                                                   const int32_t* __restrict__ pt_off,
+                                                                   const int32_t* __restrict__ np_off,
+                                                                   const int32_t* __restrict__ p_take,
+                                                                   const float* __restrict__ pair_out,
+                                                                   float* __restrict__ slot_out,
+                                                                   float* __restrict__ U_out, int64_t s_cap,
+                                                                   int64_t u_cap, double* __restrict__ loss_part,
+                                                                   int32_t* status) {
+    constexpr int J = JL<XD, D2>::J, RS = rec_stride(J), NV = 2 * J, SLOTCAP = pou_slotcap(RS);
+    __shared__ __align__(16) float table[POU_WARPS][SLOTCAP * RS];
+    __shared__ double sh[POU_WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float* T = table[w];
+    const float inv_npou = 1.0f / (float)npou;
+    double acc = 0.0;
+    const int64_t ngroups = (n + 31) / 32;
+    for (int64_t grp = (int64_t)blockIdx.x * POU_WARPS + w; grp < ngroups; grp += (int64_t)gridDim.x * POU_WARPS) {
+        const int64_t p0 = grp * 32, p = p0 + lane;
+        const bool pv = p < n;
+        const int np = (int)min((int64_t)32, n - p0);
+        const int64_t E0 = min((int64_t)pt_off[p0], s_cap), E1 = min((int64_t)pt_off[p0 + np], s_cap);
+        const int64_t U0 = np_off[p0], U1 = np_off[p0 + np];
+        const int nsl = (int)(U1 - U0);
+        const bool coop = nsl <= SLOTCAP && U1 <= u_cap;  // warp-uniform
+        float u[J], ub[J];
+#pragma unroll
+        for (int c = 0; c < J; ++c) u[c] = 0.f;
+        if (coop) {
+            for (int i = lane; i < nsl * RS; i += 32) T[i] = 0.f;
+            __syncwarp();
+            int prev = -1;  // last slot id of the previous row
+            // row loads, one row ahead of the scan
+            int nkey;
+            float nv[NV];
+            auto load_row = [&](int64_t eb) {
+                const int64_t e = eb + lane;
+                nkey = e < E1 ? p_take[e] : 0x7fffffff;
+#pragma unroll
+                for (int c = 0; c < NV; ++c) nv[c] = 0.f;
+                if (e < E1) {
+                    const float4* po = reinterpret_cast<const float4*>(pair_out + (size_t)e * RS);
+#pragma unroll
+                    for (int h = 0; h < RS / 4; ++h) {
+                        const float4 q = po[h];
+                        if (4 * h + 0 < NV) nv[4 * h + 0] = q.x;
+                        if (4 * h + 1 < NV) nv[4 * h + 1] = q.y;
+                        if (4 * h + 2 < NV) nv[4 * h + 2] = q.z;
+                        if (4 * h + 3 < NV) nv[4 * h + 3] = q.w;
+                    }
+                }
+            };
+            if (E0 < E1) load_row(E0);
+            for (int64_t eb = E0; eb < E1; eb += 32) {
+                const int64_t e = eb + lane;
+                const bool ev = e < E1;
+                const int key = nkey;
+                float v[NV];
+#pragma unroll
+                for (int c = 0; c < NV; ++c) v[c] = nv[c];
+                if (eb + 32 < E1) load_row(eb + 32);
+                // slots must ascend along the range (levels ascending within a point)
+                const int kp = __shfl_up_sync(0xffffffffu, key, 1);
+                if (ev && key < (lane ? kp : prev)) atomicOr(status, FBP_STATUS_LEVEL_ORDER);
+                prev = __shfl_sync(0xffffffffu, key, 31);
+                // inclusive scan of the records within runs of equal slot ids
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int k2 = __shfl_up_sync(0xffffffffu, key, off);
+                    const bool same = lane >= off && k2 == key;
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) {
+                        const float t = __shfl_up_sync(0xffffffffu, v[c], off);
+                        if (same) v[c] += t;
+                    }
+                }
+                const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+                if (ev && (lane == 31 || kn != key)) {  // the run's last lane adds the run's sum
+                    const int s = key - (int)U0;
+                    if (s >= 0 && s < nsl) {
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) T[s * RS + c] += v[c];
+                    } else {
+                        atomicOr(status, FBP_STATUS_BAD_INDEX);
+                    }
+                }
+                __syncwarp();
+            }
+            // per slot: U_l = N / W (quotient-rule jets) in place of N
+            for (int s = lane; s < nsl; s += 32) {
+                float N[J], W[J], Ul[J];
+#pragma unroll
+                for (int c = 0; c < J; ++c) {
+                    N[c] = T[s * RS + c];
+                    W[c] = T[s * RS + J + c];
+                }
+                quotient<XD, D2>(N, W, Ul);
+#pragma unroll
+                for (int c = 0; c < J; ++c) T[s * RS + c] = Ul[c];
+            }
+            __syncwarp();
+            if (pv) {
+                const int s0 = np_off[p] - (int)U0, s1 = np_off[p + 1] - (int)U0;
+                for (int s = s0; s < s1; ++s)
+#pragma unroll
+                    for (int c = 0; c < J; ++c) u[c] += T[s * RS + c];
+#pragma unroll
+                for (int c = 0; c < J; ++c) u[c] *= inv_npou;
+            }
+        } else if (pv) {
+            PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, s_cap, u_cap, status);
+        }
+        if (pv) acc += (double)point_residual<XD, D2>(P, inv_n, x, p, u, U_out, ub);
+        if (coop) {
+            __syncwarp();
+            if (pv) {  // seeds dL/dN_l of the point's slots, in place of U_l
+                float ubl[J];
+#pragma unroll
+                for (int c = 0; c < J; ++c) ubl[c] = ub[c] * inv_npou;
+                const int s0 = np_off[p] - (int)U0, s1 = np_off[p + 1] - (int)U0;
+                for (int s = s0; s < s1; ++s) {
+                    float W[J], Nb[J];
+#pragma unroll
+                    for (int c = 0; c < J; ++c) W[c] = T[s * RS + J + c];
+                    quotient_adj<XD, D2>(W, ubl, Nb);
+#pragma unroll
+                    for (int c = 0; c < J; ++c) T[s * RS + c] = Nb[c];
+                }
+            }
+            __syncwarp();
+            float4* dst = reinterpret_cast<float4*>(slot_out + (size_t)U0 * RS);
+            const float4* src = reinterpret_cast<const float4*>(T);
+            for (int i = lane; i < nsl * RS / 4; i += 32) dst[i] = src[i];
+            __syncwarp();
+        } else if (pv) {
+            PointPOU<XD, D2>::seed(p, npou, np_off, ub, slot_out, u_cap);
+        }
+    }
+    // block sum of the squared residuals (FP64), fixed order
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) sh[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < POU_WARPS; ++q) t += sh[q];
+        loss_part[blockIdx.x] = t;
+    }
 }
 
 __global__ void loss_finalize_kernel(const double* __restrict__ part, int np, double scale, double* loss) {
@@ -592,13 +748,16 @@ extern "C" int fbp_pou_loss(int32_t xd, int32_t d2mask, const fbp_problem* prob,
                 "fbp_pou_loss: bad args");
     FBP_REQUIRE(n > 0, FBP_ERR_INVALID, "fbp_pou_loss: no points");
     FBP_REQUIRE(prob->ng == 0 || prob->gauss, FBP_ERR_INVALID, "fbp_pou_loss: null gaussians");
-    const int g = grid_pts(n);
+    // CTAs of POU_WARPS warps, each warp 32 points at a time
+    const int64_t ctas = ((n + 31) / 32 + POU_WARPS - 1) / POU_WARPS;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ctas, (int64_t)sm_count() * 8));
     FBP_REQUIRE(n_part >= g, FBP_ERR_CAPACITY, "fbp_pou_loss: n_part=%d < grid %d", n_part, g);
     cudaStream_t st = as_stream(stream);
     const float inv_n = (float)(1.0 / (double)n);
 #define X(a, b)                                                                                              \
     if (xd == a && d2mask == b) {                                                                            \
-        pou_loss_kernel<a, b><<<g, POU_T, 0, st>>>(*prob, n, npou, inv_n, x, pt_off, np_off, p_take, pair_out, \
+        pou_loss_kernel<a, b><<<g, POU_WARPS * 32, 0, st>>>(*prob, n, npou, inv_n, x, pt_off, np_off, p_take,   \
+                                                             pair_out,                                        \
                                                     slot_out, U_out, s_cap, u_cap, loss_part, status);      \
         FBP_LAUNCH_CHECK();                                                                                  \
         if (n_part > g) FBP_CUDA_CHECK(cudaMemsetAsync(loss_part + g, 0, (n_part - g) * sizeof(double), st)); \

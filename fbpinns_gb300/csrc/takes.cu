@@ -132,22 +132,8 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
                 e1 = b.cell_start[c + 1];
             }
             int64_t k = 0;
-            for (;;) {
-                // next hit: from the mask, or by testing the next candidates
-                int j;
-                if (cand >= 0) {
-                    if (!hit) break;
-                    j = b.cell_boxes[cand + __ffsll((long long)hit) - 1];
-                    hit &= hit - 1;
-                } else {
-                    for (; e < e1; ++e) {
-                        j = b.cell_boxes[e];
-                        if ((!b.select || b.select[j]) && inside_box<XD>(xp, b.xmins, b.xmaxs, j)) break;
-                    }
-                    if (e >= e1) break;
-                    ++e;
-                }
-                const int lv = b.pou[j] & 63;
+            // the point's k-th pair (box j at POU level lv): staged or written directly
+            auto emit = [&](int j, int lv) {
                 const int64_t q = base + k - wb;
                 if (staged) {
                     if (q >= 0 && q < total)
@@ -166,6 +152,30 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
                     }
                 }
                 ++k;
+            };
+            if (cand >= 0) {
+                // hits from the mask, four at a time so that their loads overlap
+                while (hit) {
+                    int jj[4], ll[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        jj[u] = -1;
+                        if (hit) {
+                            jj[u] = b.cell_boxes[cand + __ffsll((long long)hit) - 1];
+                            hit &= hit - 1;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) ll[u] = jj[u] >= 0 ? (b.pou[jj[u]] & 63) : 0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (jj[u] >= 0) emit(jj[u], ll[u]);
+                }
+            } else {
+                for (; e < e1; ++e) {
+                    const int j = b.cell_boxes[e];
+                    if ((!b.select || b.select[j]) && inside_box<XD>(xp, b.xmins, b.xmaxs, j)) emit(j, b.pou[j] & 63);
+                }
             }
             // unique (point, level) slots in ascending level order
             const int nl = __popcll(lvl);
