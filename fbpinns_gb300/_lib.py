@@ -24,6 +24,16 @@ STATUS_BITS = {
 
 PROBLEM_NONE, PROBLEM_HO_HARDBC, PROBLEM_BURGERS, PROBLEM_POISSON2D, PROBLEM_WAVE_C, PROBLEM_HELMHOLTZ2D = range(6)
 D2_LAPLACIAN = 8  # FBP_D2_LAPLACIAN: one jet slot for the sum of the masked second derivatives
+
+
+def D2_GROUP(dims):
+    """FBP_D2_GROUP: the masked dims in ``dims`` share one jet slot (their sum)."""
+    return (int(dims) & 7) << 4
+
+
+def d2_group(d2):
+    """Dims summed into the group's jet slot of a d2mask (0: no group)."""
+    return (d2 & 7) if d2 & D2_LAPLACIAN else ((d2 >> 4) & 7 & d2)
 ACT_TANH, ACT_SIN = 0, 1  # FBP_ACT_*: hidden-layer activation of the compiled networks
 ACTIVATIONS = {"tanh": ACT_TANH, "sin": ACT_SIN}
 

@@ -43,11 +43,18 @@ __host__ __device__ constexpr int popc_const(int v) {
 }
 
 // Second-derivative part of a jet, from the d2mask: bits 0-2 name the dims
-// whose pure second derivatives are needed; with FBP_D2_LAPLACIAN (bit 3) set,
-// one slot holds their sum (the Laplacian over those dims, propagated directly
-// as in the forward-Laplacian scheme) instead of one slot per dim.
-__host__ __device__ constexpr bool d2_lap(int d2) { return (d2 & FBP_D2_LAPLACIAN) != 0; }
-__host__ __device__ constexpr int d2_slots(int d2) { return d2_lap(d2) ? ((d2 & 7) ? 1 : 0) : popc_const(d2 & 7); }
+// whose pure second derivatives are needed.  The dims of the group (all of
+// them with FBP_D2_LAPLACIAN, bit 3; else the dims named by bits 4-6, see
+// FBP_D2_GROUP) share one slot that holds the sum of their second
+// derivatives (a Laplacian, propagated directly as in the forward-Laplacian
+// scheme); every other masked dim has a slot of its own.  Slot order: the
+// group's slot first, then the single dims ascending.
+__host__ __device__ constexpr int d2_group(int d2) {
+    return (d2 & FBP_D2_LAPLACIAN) ? (d2 & 7) : ((d2 >> 4) & 7 & d2);
+}
+__host__ __device__ constexpr int d2_singles(int d2) { return d2 & 7 & ~d2_group(d2); }
+__host__ __device__ constexpr bool d2_lap(int d2) { return d2_group(d2) != 0; }
+__host__ __device__ constexpr int d2_slots(int d2) { return (d2_group(d2) ? 1 : 0) + popc_const(d2_singles(d2)); }
 
 // Jet layout: [u, d/dx_0..d/dx_{XD-1}, then the second-derivative slots: one
 // per bit i of the d2mask ascending, or the single Laplacian slot].
@@ -77,10 +84,11 @@ struct DimsOf {
 };
 
 // Dims whose pure second derivatives second-derivative slot s of a d2mask sums
-// (one dim per slot, or all masked dims for the Laplacian slot).
+// (the group for the group's slot, else one dim).
 template <int D2>
 __host__ __device__ constexpr int d2_slot_dims(int s) {
-    return d2_lap(D2) ? (D2 & 7) : (1 << DimsOf<D2 & 7>::get(s));
+    return d2_group(D2) ? (s == 0 ? d2_group(D2) : (1 << DimsOf<d2_singles(D2)>::get(s - 1)))
+                        : (1 << DimsOf<D2 & 7>::get(s));
 }
 
 // tanh from the identity tanh|x| = (1 - e) / (1 + e), e = exp(-2|x|), with the
@@ -92,11 +100,6 @@ __device__ __forceinline__ float tanh_fast(float x) {
     return copysignf(__fdividef(1.0f - e, 1.0f + e), x);
 }
 
-inline int jet_size_rt(int xd, int d2) {
-    int c = 0;
-    for (int i = 0; i < xd; ++i) c += (d2 >> i) & 1;
-    if (d2_lap(d2)) c = c ? 1 : 0;
-    return 1 + xd + c;
-}
+inline int jet_size_rt(int xd, int d2) { return 1 + xd + d2_slots(d2); }
 
 }  // namespace fbp

@@ -18,19 +18,21 @@ namespace fbp {
 
 template <int XD, int D2>
 struct JL {
-    static constexpr bool LAP = d2_lap(D2);
-    static constexpr int M = D2 & 7;
+    static constexpr int M = D2 & 7;           // dims with second derivatives
+    static constexpr int G = d2_group(D2);     // dims summed in the group's slot
+    static constexpr int SG = d2_singles(D2);  // dims with a slot each
     static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
     // dims whose pure second derivatives slot s sums
     __host__ __device__ static constexpr int slot_dims(int s) { return d2_slot_dims<D2>(s); }
     // component of the pure second derivative along d (-1 if absent or summed)
-    static constexpr int S0 = (!LAP && ((M >> 0) & 1)) ? 1 + XD : -1;
-    static constexpr int S1 = (!LAP && ((M >> 1) & 1)) ? 1 + XD + popc_const(M & 1) : -1;
-    static constexpr int S2 = (!LAP && ((M >> 2) & 1)) ? 1 + XD + popc_const(M & 3) : -1;
+    static constexpr int SB = 1 + XD + (G ? 1 : 0);  // first single-dim slot
+    static constexpr int S0 = ((SG >> 0) & 1) ? SB : -1;
+    static constexpr int S1 = ((SG >> 1) & 1) ? SB + popc_const(SG & 1) : -1;
+    static constexpr int S2 = ((SG >> 2) & 1) ? SB + popc_const(SG & 3) : -1;
     __host__ __device__ static constexpr int sidx(int d) { return d == 0 ? S0 : (d == 1 ? S1 : S2); }
-    // component of the Laplacian over the masked dims (-1 without FBP_D2_LAPLACIAN)
-    static constexpr int LAPI = (LAP && M) ? 1 + XD : -1;
+    // component of the group's sum of second derivatives (-1 without a group)
+    static constexpr int LAPI = G ? 1 + XD : -1;
 };
 
 template <int XD, int D2>
@@ -240,7 +242,7 @@ __device__ __forceinline__ float residual(const fbp_problem& P, const float* xp,
             break;
         }
         case FBP_PROBLEM_POISSON2D: {  // u_xx + u_yy + f
-            if constexpr (XD == 2 && L::LAPI > 0 && L::M == 3) {
+            if constexpr (XD == 2 && L::LAPI > 0 && L::G == 3) {
                 float f = 0.f;
                 for (int k = 1; k <= P.n_int; ++k) {
                     const float a = (float)(1 << k);
@@ -262,7 +264,7 @@ __device__ __forceinline__ float residual(const fbp_problem& P, const float* xp,
             break;
         }
         case FBP_PROBLEM_HELMHOLTZ2D: {  // u_xx + u_yy + k^2 u + f
-            if constexpr (XD == 2 && L::LAPI > 0 && L::M == 3) {
+            if constexpr (XD == 2 && L::LAPI > 0 && L::G == 3) {
                 const float k = P.p[1];
                 float f = 0.f;
                 for (int g = 0; g < P.ng; ++g) {
@@ -290,6 +292,12 @@ __device__ __forceinline__ float residual(const fbp_problem& P, const float* xp,
             break;
         }
         case FBP_PROBLEM_WAVE_C: {  // problems.py:401-405: u_xx + u_yy - u_tt / c^2
+            if constexpr (XD == 3 && L::LAPI > 0 && L::G == 3 && L::sidx(2) > 0) {  // (u_xx + u_yy), u_tt
+                const float ic2 = 1.0f / (P.p[0] * P.p[0]);
+                r = u[L::LAPI] - ic2 * u[L::sidx(2)];
+                dr[L::LAPI] = 1.f;
+                dr[L::sidx(2)] = -ic2;
+            }
             if constexpr (XD == 3 && L::sidx(0) > 0 && L::sidx(1) > 0 && L::sidx(2) > 0) {
                 const float ic2 = 1.0f / (P.p[0] * P.p[0]);
                 r = u[L::sidx(0)] + u[L::sidx(1)] - ic2 * u[L::sidx(2)];
@@ -691,7 +699,7 @@ struct XDispatch;
 
 #define FBP_XD_D2_CASES(X) \
     X(1, 0) X(1, 1) X(2, 0) X(2, 1) X(2, 2) X(2, 3) X(2, 11) X(3, 0) X(3, 1) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6) \
-        X(3, 7)
+        X(3, 7) X(3, 55)
 
 static int grid_pts(int64_t n) {
     int64_t b = (n + POU_T - 1) / POU_T;

@@ -68,24 +68,25 @@ def jet_index(xd, d2mask, ixs):
         return 0
     if len(ixs) == 1:
         return 1 + ixs[0]
-    if d2mask & _lib.D2_LAPLACIAN:
-        raise ValueError("a Laplacian jet (FBP_D2_LAPLACIAN) holds no single second derivative")
     d = ixs[0]
-    return 1 + xd + bin(d2mask & ((1 << d) - 1)).count("1")
+    group = _lib.d2_group(d2mask)
+    if (group >> d) & 1:
+        raise ValueError(f"d2mask {d2mask} sums d2/dx{d}^2 into its group slot (no single component)")
+    singles = d2mask & 7 & ~group
+    return 1 + xd + (1 if group else 0) + bin(singles & ((1 << d) - 1)).count("1")
 
 
 def laplacian_index(xd, d2mask):
-    """Component holding the sum of the masked pure second derivatives, for a
-    d2mask with FBP_D2_LAPLACIAN."""
-    if not d2mask & _lib.D2_LAPLACIAN or not d2mask & 7:
+    """Component holding the sum of the group's pure second derivatives
+    (FBP_D2_LAPLACIAN or FBP_D2_GROUP)."""
+    if not _lib.d2_group(d2mask):
         raise ValueError(f"d2mask {d2mask} has no Laplacian slot")
     return 1 + xd
 
 
 def jet_size(xd, d2mask):
-    if d2mask & _lib.D2_LAPLACIAN:
-        return 1 + xd + (1 if d2mask & 7 else 0)
-    return 1 + xd + bin(d2mask).count("1")
+    group = _lib.d2_group(d2mask)
+    return 1 + xd + (1 if group else 0) + bin(d2mask & 7 & ~group).count("1")
 
 
 def record_stride(J):

@@ -262,7 +262,8 @@ class WaveEquationConstantVelocity3D(Problem):
         p = all_params["static"]["problem"]
         src = p["source"]
         t1 = float(src[:, 2].min()) / float(p["c0"])
-        return {"kind": _lib.PROBLEM_WAVE_C, "p": [float(p["c0"]), t1], "n_int": 0, "gauss": src}
+        return {"kind": _lib.PROBLEM_WAVE_C, "p": [float(p["c0"]), t1], "n_int": 0, "gauss": src,
+                "d2_group": 3}  # the residual needs u_xx + u_yy and u_tt
 
 
 class WaveEquationGaussianVelocity3D(WaveEquationConstantVelocity3D):
@@ -333,7 +334,7 @@ class Poisson2D(Problem):
     def fused_spec(cls, all_params):
         p = all_params["static"]["problem"]
         return {"kind": _lib.PROBLEM_POISSON2D, "p": [p["sd"]], "n_int": p["n_freq"], "gauss": None,
-                "laplacian": True}
+                "d2_group": 3}  # the residual needs only u_xx + u_yy
 
 
 def seeded_gaussians(n, seed, centre=(0.1, 0.9), width=(0.02, 0.1), amp=(-1.0, 1.0)):
@@ -378,4 +379,4 @@ class Helmholtz2D(Problem):
     def fused_spec(cls, all_params):
         p = all_params["static"]["problem"]
         return {"kind": _lib.PROBLEM_HELMHOLTZ2D, "p": [p["sd"], p["k"]], "n_int": 0, "gauss": p["source"],
-                "laplacian": True}
+                "d2_group": 3}  # the residual needs only u_xx + u_yy

@@ -270,10 +270,13 @@ class FBPINNTrainer:
         spec = problem.fused_spec(all_params) if c.engine == "fused" else None
         single = len(constraints_global) == 1 and not all_params["trainable"].get("problem")
         use_fused = spec is not None and single
-        if use_fused and spec.get("laplacian") and d2 and _lib.load().fbp_has_shape(
-                xd, layer_sizes[1], layer_sizes[2] if len(layer_sizes) == 4 else 0, d2 | _lib.D2_LAPLACIAN,
-                _lib.ACTIVATIONS[activation]):
-            d2 |= _lib.D2_LAPLACIAN  # the residual needs only the Laplacian: one jet slot for it
+        group = spec.get("d2_group", 0) if use_fused else 0
+        if group and (d2 & group) == group:
+            # the residual uses these second derivatives only through their sum: one jet slot for it
+            d2g = d2 | (_lib.D2_LAPLACIAN if group == (d2 & 7) else _lib.D2_GROUP(group))
+            if _lib.load().fbp_has_shape(xd, layer_sizes[1], layer_sizes[2] if len(layer_sizes) == 4 else 0, d2g,
+                                         _lib.ACTIVATIONS[activation]):
+                d2 = d2g
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
                            tensor_cores=getattr(c, "tensor_cores", None), activation=activation)
         eng.set_theta(pack_layers(net_tr["layers"]))

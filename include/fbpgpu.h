@@ -53,6 +53,11 @@ extern "C" {
  * instead of one slot per dim.  Enough for residuals that use only that sum
  * (Poisson, Helmholtz); the jet then has 1 + xd + 1 components. */
 #define FBP_D2_LAPLACIAN 8
+/* d2mask group (without FBP_D2_LAPLACIAN): the masked dims in `dims` share
+ * one slot (the sum of their second derivatives, first), the other masked
+ * dims keep a slot each; e.g. 7 | FBP_D2_GROUP(3) carries u_xx + u_yy and
+ * u_tt for the wave residual u_xx + u_yy - u_tt / c^2. */
+#define FBP_D2_GROUP(dims) (((dims) & 7) << 4)
 
 /* Hidden-layer activations of the compiled networks (fbp_net.act). */
 #define FBP_ACT_TANH 0   /* FCN (fbpinns/networks.py:61-68) */

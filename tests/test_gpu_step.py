@@ -104,11 +104,12 @@ def _oracle_loss_grad(name, static, layers64, x, prob_static):
 
 
 @pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("burgers", False), ("poisson", False),
-                                      ("poisson", True), ("wave", False), ("helmholtz", False),
+                                      ("poisson", True), ("wave", False), ("wave", True), ("helmholtz", False),
                                       ("helmholtz", True)])
 def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     """Fused loss and per-subdomain gradients vs the float64 oracle.  lap=True
-    carries one Laplacian jet slot (u_xx + u_yy) instead of u_xx and u_yy."""
+    carries one jet slot for u_xx + u_yy instead of u_xx and u_yy (the wave
+    keeps u_tt in a slot of its own)."""
     recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
     static = decomposition(recipe)
     layers64 = random_layers(ls, static["m"], seed=5)
@@ -117,7 +118,7 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     prob_static = pcls.init_params(**pkw)[0]
     loss_ref, g_ref, a_ims, active = _oracle_loss_grad(name, static, layers32, x, prob_static)
     assert d2mask_of([_required(name)], x.shape[1]) | d2 == d2
-    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0))
+    eng = _engine(static, layers32, d2 | (0 if not lap else _lib.D2_LAPLACIAN if d2 == 3 else _lib.D2_GROUP(3)))
     eng.set_state(active)
     eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
     ps = eng.points(torch.tensor(x))
@@ -180,6 +181,25 @@ def test_laplacian_jets_match_sum_of_second_derivatives(cuda):
         for c in range(3):
             assert rel_err(L[:, c], U[:, c]) < JET_TOL, (ls, c)
         assert rel_err(L[:, 3], U[:, 3] + U[:, 4]) < JET_TOL, ls
+
+
+def test_grouped_wave_jets_match_per_dim_jets(cuda):
+    """7 | FBP_D2_GROUP(3): the jet carries u_xx + u_yy and u_tt; they equal
+    the per-dim jet's components (FP32 rounding only)."""
+    static = decomposition("wave")
+    layers = random_layers([3, 8, 8, 1], static["m"], seed=33)
+    g = np.random.default_rng(8)
+    x = torch.tensor(g.uniform([-1, -1, 0], [1, 1, 1], (3000, 3)).astype(np.float32))
+    Us = []
+    for d2 in (7, 7 | _lib.D2_GROUP(3)):
+        eng = _engine(static, layers, d2)
+        Us.append(FBPINNJet.apply(eng.theta, eng, eng.points(x)).double().cpu().numpy())
+    U, G = Us
+    assert U.shape[1] == 7 and G.shape[1] == 6
+    for c in range(4):
+        assert rel_err(G[:, c], U[:, c]) < JET_TOL, c
+    assert rel_err(G[:, 4], U[:, 4] + U[:, 5]) < JET_TOL
+    assert rel_err(G[:, 5], U[:, 6]) < JET_TOL
 
 
 def test_generic_path_matches_fused(cuda):

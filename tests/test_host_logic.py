@@ -231,6 +231,21 @@ def test_cell_grid_registers_every_containing_box():
         assert np.all(np.diff(seg) > 0)
 
 
+def test_jet_layout_with_second_derivative_groups():
+    """Jet component layout for per-dim, Laplacian and grouped d2masks."""
+    from fbpinns_gb300 import _lib
+    from fbpinns_gb300.engine import jet_index, jet_size, laplacian_index
+    assert jet_size(2, 3) == 5 and jet_index(2, 3, (1, 1)) == 4
+    lap = 3 | _lib.D2_LAPLACIAN
+    assert jet_size(2, lap) == 4 and laplacian_index(2, lap) == 3
+    with pytest.raises(ValueError):
+        jet_index(2, lap, (0, 0))
+    wave = 7 | _lib.D2_GROUP(3)
+    assert _lib.d2_group(wave) == 3 and jet_size(3, wave) == 6
+    assert laplacian_index(3, wave) == 4 and jet_index(3, wave, (2, 2)) == 5
+    assert jet_index(3, wave, (0,)) == 1 and jet_index(3, 7, (2, 2)) == 6
+
+
 def test_constants_key_checking_and_defaults():
     c = Constants(n_steps=3)
     assert c.n_steps == 3 and c["sampler"] == "grid"
