@@ -52,10 +52,10 @@ def FBPINN_solution(c, all_params, active, x_batch):
     from .trainers import FBPINNTrainer, NETWORK_ACTIVATIONS
     ap = _torch_tree(all_params)
     layers = ap["trainable"]["network"]["subdomain"]["layers"]
-    sizes = [layers[0][0].shape[2]] + [w.shape[1] for w, _ in layers]
+    sizes = [layers[0][0].shape[2]] + [layer[0].shape[1] for layer in layers]
     act = NETWORK_ACTIVATIONS.get(c.network, "tanh")
     eng = FBPINNEngine(ap["static"]["decomposition"], sizes, inference_d2mask(sizes, act), activation=act)
-    eng.set_theta(pack_layers([(torch.as_tensor(w), torch.as_tensor(b)) for w, b in layers]))
+    eng.set_theta(pack_layers([tuple(torch.as_tensor(t) for t in layer) for layer in layers]))
     dev = eng.device
     ap["static"]["problem"] = {k: (v.to(dev) if torch.is_tensor(v) else v) for k, v in ap["static"]["problem"].items()}
     return FBPINNTrainer.predict(eng, ap, c.problem, torch.as_tensor(x_batch, dtype=torch.float32))

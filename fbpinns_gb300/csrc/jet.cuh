@@ -17,59 +17,109 @@
 
 namespace fbp {
 
-// Hidden-layer activations (fbp_net.act) and their jet rules.  Each keeps one
-// value per first-layer neuron in shared memory ("stored") from which the
-// value and the first two derivatives are recovered; zbar0 is the adjoint of
-// the jet map (a, a', a'') at z for the incoming sensitivities of a, a', a''.
+// Hidden-layer activations (fbp_net.act): sigma(z) = c f(o z) per neuron, with
+// c = o = 1 for the plain FCN and SIREN.  Each keeps one value per first-layer
+// neuron in shared memory ("stored": tanh z for the plain tanh, else z) from
+// which derivs recovers sigma and its first three derivatives; pgrad gives
+// the gradient of the adaptive parameters from the sensitivities of
+// (sigma, sigma', sigma'') at z.
 template <int ACT>
 struct Act;
 
 template <>
-struct Act<FBP_ACT_TANH> {  // FCN (fbpinns/networks.py:61-68): stored a = tanh z
-    __device__ __forceinline__ static float stored(float z) { return tanh_fast(z); }
-    __device__ __forceinline__ static void derivs(float s, float& a, float& d1, float& d2) {
+struct Act<FBP_ACT_TANH> {  // FCN (fbpinns/networks.py:61-68)
+    static constexpr int EXTRA = 0;  // trainable parameters per neuron besides W, b
+    __device__ __forceinline__ static float stored(float z, float) { return tanh_fast(z); }
+    __device__ __forceinline__ static void derivs(float s, float, float, float& a, float& d1, float& d2, float& d3) {
         a = s;
         d1 = 1.0f - a * a;
         d2 = -2.0f * a * d1;
-    }
-    __device__ __forceinline__ static void eval(float z, float& a, float& d1, float& d2) { derivs(tanh_fast(z), a, d1, d2); }
-    // third derivative of tanh: tanh' (6 a^2 - 2)
-    __device__ __forceinline__ static float zbar0(float ab, float d1b, float d2b, float a, float d1, float) {
-        return (ab + d1b * (-2.0f * a) + d2b * (6.0f * a * a - 2.0f)) * d1;
+        d3 = d1 * (6.0f * a * a - 2.0f);
     }
 };
 
 template <>
-struct Act<FBP_ACT_SIN> {  // SIREN (fbpinns/networks.py:102-131): stored z
-    __device__ __forceinline__ static float stored(float z) { return z; }
-    __device__ __forceinline__ static void derivs(float s, float& a, float& d1, float& d2) {
+struct Act<FBP_ACT_SIN> {  // SIREN (fbpinns/networks.py:102-131)
+    static constexpr int EXTRA = 0;
+    __device__ __forceinline__ static float stored(float z, float) { return z; }
+    __device__ __forceinline__ static void derivs(float s, float, float, float& a, float& d1, float& d2, float& d3) {
         float sn, cs;
         sincosf(s, &sn, &cs);
         a = sn;
         d1 = cs;
         d2 = -sn;
-    }
-    __device__ __forceinline__ static void eval(float z, float& a, float& d1, float& d2) { derivs(z, a, d1, d2); }
-    // third derivative of sin: -cos
-    __device__ __forceinline__ static float zbar0(float ab, float d1b, float d2b, float, float d1, float d2) {
-        return ab * d1 + d1b * d2 - d2b * d1;
+        d3 = -cs;
     }
 };
+
+template <>
+struct Act<FBP_ACT_ADAPTIVE_TANH> {  // AdaptiveFCN (fbpinns/networks.py:70-100): a tanh(z / a)
+    static constexpr int EXTRA = 1;  // a; here c = a, o = 1 / a
+    __device__ __forceinline__ static float stored(float z, float) { return z; }
+    __device__ __forceinline__ static void derivs(float s, float c, float o, float& a, float& d1, float& d2,
+                                                  float& d3) {
+        const float t = tanh_fast(o * s), f1 = 1.0f - t * t;
+        a = c * t;
+        d1 = c * o * f1;
+        d2 = -2.0f * c * o * o * t * f1;
+        d3 = c * o * o * o * f1 * (6.0f * t * t - 2.0f);
+    }
+};
+
+template <>
+struct Act<FBP_ACT_ADAPTIVE_SIN> {  // AdaptiveSIREN (fbpinns/networks.py:133-163): c sin(o z)
+    static constexpr int EXTRA = 2;  // c, o
+    __device__ __forceinline__ static float stored(float z, float) { return z; }
+    __device__ __forceinline__ static void derivs(float s, float c, float o, float& a, float& d1, float& d2,
+                                                  float& d3) {
+        float sn, cs;
+        sincosf(o * s, &sn, &cs);
+        a = c * sn;
+        d1 = c * o * cs;
+        d2 = -c * o * o * sn;
+        d3 = -c * o * o * o * cs;
+    }
+};
+
+// Gradient of the adaptive parameters of one neuron for one pair, from the
+// sensitivities ab, d1b, d2b of sigma, sigma', sigma'' at the pre-activation z:
+//   dL/dc = (ab sigma + d1b sigma' + d2b sigma'') / c
+//   dL/do = (ab z sigma' + d1b (sigma' + z sigma'') + d2b (2 sigma'' + z sigma''')) / o
+// AdaptiveFCN (c = a, o = 1/a): dL/da = dL/dc - o^2 dL/do;  AdaptiveSIREN: (dL/dc, dL/do).
+template <int ACT>
+__device__ __forceinline__ void act_param_grad(float ab, float d1b, float d2b, float z, float a, float d1, float d2,
+                                               float d3, float c, float o, float (&g)[Act<ACT>::EXTRA > 0 ? Act<ACT>::EXTRA : 1]) {
+    if constexpr (Act<ACT>::EXTRA > 0) {
+        const float gc = (ab * a + d1b * d1 + d2b * d2) / c;
+        const float go = (ab * z * d1 + d1b * (d1 + z * d2) + d2b * (2.0f * d2 + z * d3)) / o;
+        if constexpr (ACT == FBP_ACT_ADAPTIVE_TANH) {
+            g[0] = gc - o * o * go;
+        } else {
+            g[0] = gc;
+            g[1] = go;
+        }
+    }
+}
 
 template <int XD_, int H1_, int H2_, int D2_, int ACT_ = FBP_ACT_TANH>
 struct Cfg {
     static constexpr int XD = XD_, H1 = H1_, H2 = H2_, D2 = D2_, ACT = ACT_;
     using AF = Act<ACT_>;
+    static constexpr int EXTRA = AF::EXTRA;  // per-neuron activation parameters of every layer
     static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
     static constexpr bool TWO = H2 > 0;
     static constexpr int HL = TWO ? H2 : H1;  // width feeding the output layer
-    static constexpr int oW1 = 0, ob1 = H1 * XD;
-    static constexpr int oW2 = ob1 + H1;
+    // packed layout per layer: W (fan_out, fan_in), b (fan_out), then EXTRA
+    // vectors (fan_out) of activation parameters (the output layer's unused)
+    static constexpr int oW1 = 0, ob1 = H1 * XD, oX1 = ob1 + H1;
+    static constexpr int oW2 = oX1 + EXTRA * H1;
     static constexpr int ob2 = oW2 + (TWO ? H2 * H1 : 0);
-    static constexpr int oW3 = TWO ? ob2 + H2 : ob1 + H1;
+    static constexpr int oX2 = ob2 + (TWO ? H2 : 0);
+    static constexpr int oW3 = TWO ? oX2 + EXTRA * H2 : oX1 + EXTRA * H1;
     static constexpr int ob3 = oW3 + HL;
-    static constexpr int P = ob3 + 1;
+    static constexpr int oX3 = ob3 + 1;
+    static constexpr int P = oX3 + EXTRA;
     static constexpr int KC = TWO ? (H2 < 16 ? H2 : 16) : 1;  // layer-2 neurons per register pass
     static constexpr int NCH = TWO ? H2 / KC : 1;
     static_assert(!TWO || H2 % KC == 0, "H2 must be a multiple of the chunk");
@@ -94,9 +144,24 @@ struct SParams {
     float b2[C::TWO ? C::H2 : 4];
     float W3[C::HL];
     float b3;
+    // activation parameters sigma(z) = c f(o z) of the hidden neurons (adaptive networks)
+    float ac1[C::EXTRA > 0 ? C::H1 : 1], ao1[C::EXTRA > 0 ? C::H1 : 1];
+    float ac2[C::EXTRA > 0 && C::TWO ? C::H2 : 1], ao2[C::EXTRA > 0 && C::TWO ? C::H2 : 1];
     float mu[C::XD], inv_sd[C::XD], wsc[C::XD];  // wsc = pi / (2 sd)
     float flag, mu_u, sd_u;
 };
+
+// the (c, o) of hidden neuron n of layer 1 (L2 = false) or 2 (L2 = true)
+template <class C, bool L2>
+__device__ __forceinline__ float act_c(const SParams<C>& S, int n) {
+    if constexpr (C::EXTRA == 0) return 1.0f;
+    else return L2 ? S.ac2[n] : S.ac1[n];
+}
+template <class C, bool L2>
+__device__ __forceinline__ float act_o(const SParams<C>& S, int n) {
+    if constexpr (C::EXTRA == 0) return 1.0f;
+    else return L2 ? S.ao2[n] : S.ao1[n];
+}
 
 // Subdomain j's weights into shared memory (W2T: also the transposed W2 that
 // the CUDA-core layer-2 loops read).
@@ -115,6 +180,21 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
         for (int i = threadIdx.x; i < C::H2; i += blockDim.x) S.b2[i] = th[C::ob2 + i];
     }
     for (int i = threadIdx.x; i < C::HL; i += blockDim.x) S.W3[i] = th[C::oW3 + i];
+    if constexpr (C::EXTRA > 0) {
+        // AdaptiveFCN: a (c = a, o = 1/a); AdaptiveSIREN: c then o
+        for (int i = threadIdx.x; i < C::H1; i += blockDim.x) {
+            const float v = th[C::oX1 + i];
+            S.ac1[i] = v;
+            S.ao1[i] = C::EXTRA == 1 ? 1.0f / v : th[C::oX1 + C::H1 + i];
+        }
+        if constexpr (C::TWO) {
+            for (int i = threadIdx.x; i < C::H2; i += blockDim.x) {
+                const float v = th[C::oX2 + i];
+                S.ac2[i] = v;
+                S.ao2[i] = C::EXTRA == 1 ? 1.0f / v : th[C::oX2 + C::H2 + i];
+            }
+        }
+    }
     if (threadIdx.x == 0) {
         S.b3 = th[C::ob3];
         S.flag = net.flags[j];
@@ -148,22 +228,23 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
     }
 }
 
-// Jet of one first-layer neuron's activation from a = tanh(z1).
+// Jet of first-layer neuron n's activation from its stored value s.
 template <class C>
-__device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float a, float (&v)[C::J]) {  // a: stored value
-    float tp, tpp;
-    C::AF::derivs(a, v[0], tp, tpp);
+__device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float s, float (&v)[C::J]) {
+    float tp, tpp, tppp;
+    C::AF::derivs(s, act_c<C, false>(S, n), act_o<C, false>(S, n), v[0], tp, tpp, tppp);
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) v[1 + d] = tp * S.cw[n * C::XD + d];
 #pragma unroll
     for (int s = 0; s < C::NS; ++s) v[1 + C::XD + s] = tpp * S.c2[n * C::NS + s];
 }
 
-// tanh applied to a z-jet.
+// The activation (parameters c, o) applied to a z-jet; a, tp, tpp, tppp are
+// sigma and its first three derivatives at z[0].
 template <class C>
-__device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J], float& a, float& tp,
-                                         float& tpp) {
-    C::AF::eval(z[0], a, tp, tpp);
+__device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J], float& a, float& tp, float& tpp,
+                                         float& tppp, float c = 1.0f, float o = 1.0f) {
+    C::AF::derivs(C::AF::stored(z[0], o), c, o, a, tp, tpp, tppp);
     g[0] = a;
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) g[1 + d] = tp * z[1 + d];
@@ -177,11 +258,13 @@ __device__ __forceinline__ void tanh_jet(const float (&z)[C::J], float (&g)[C::J
     }
 }
 
-// Adjoint of tanh_jet: given g-bar, returns z-bar (in place of gb).
+// Adjoint of tanh_jet: given g-bar, returns z-bar and the sensitivities tpb,
+// tppb of sigma', sigma'' (for the adaptive parameters' gradient).
 template <class C>
-__device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float a, float tp, float tpp,
-                                             float (&gb)[C::J], float (&zb)[C::J]) {
-    float tpb = 0.f, tppb = 0.f;
+__device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float tp, float tpp, float tppp,
+                                             float (&gb)[C::J], float (&zb)[C::J], float& tpb, float& tppb) {
+    tpb = 0.f;
+    tppb = 0.f;
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) {
         tpb += gb[1 + d] * z[1 + d];
@@ -200,7 +283,7 @@ __device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float a, fl
                 zb[1 + d] += g2 * z[1 + d];
             }
     }
-    zb[0] = C::AF::zbar0(gb[0], tpb, tppb, a, tp, tpp);
+    zb[0] = gb[0] * tp + tpb * tpp + tppb * tppp;
 }
 
 // Window jet (cosine window of fbpinns/windows.py:25-35 times flag plus 1-flag):
@@ -296,7 +379,7 @@ __device__ __forceinline__ float l1_act(const SParams<C>& S, const float (&xn)[C
     float z = S.b1[n];
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) z = fmaf(S.W1[n * C::XD + d], xn[d], z);
-    return C::AF::stored(z);
+    return C::AF::stored(z, act_o<C, false>(S, n));
 }
 
 // Layer-2 z-jets for neurons [k0, k0+KC) from first-layer activations a1row[n*stride]
@@ -341,9 +424,10 @@ __device__ __forceinline__ void net_jet(const SParams<C>& S, const float (&xn)[C
             l2_chunk<C>(S, a1row, stride, ch * C::KC, acc);
 #pragma unroll
             for (int k = 0; k < C::KC; ++k) {
-                float g[C::J], a, tp, tpp;
-                tanh_jet<C>(acc[k], g, a, tp, tpp);
-                const float w3 = S.W3[ch * C::KC + k];
+                const int kk = ch * C::KC + k;
+                float g[C::J], a, tp, tpp, tppp;
+                tanh_jet<C>(acc[k], g, a, tp, tpp, tppp, act_c<C, true>(S, kk), act_o<C, true>(S, kk));
+                const float w3 = S.W3[kk];
 #pragma unroll
                 for (int c = 0; c < C::J; ++c) out[c] = fmaf(w3, g[c], out[c]);
             }
@@ -467,6 +551,9 @@ struct __align__(16) WarpRows {
     float gb2[C::TWO ? C::H2 : 4];
     float gW3[C::HL];
     float gb3;
+    // activation-parameter gradients of the hidden layers (adaptive networks)
+    float gX1[C::EXTRA > 0 ? C::EXTRA * C::H1 : 4];
+    float gX2[C::EXTRA > 0 && C::TWO ? C::EXTRA * C::H2 : 4];
 };
 
 // Reduce-scatter over the warp: v[NV] per lane -> lane L holds the warp sums of
@@ -517,6 +604,11 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             for (int i = lane; i < H2; i += 32) R.gb2[i] = 0.f;
         for (int i = lane; i < HL; i += 32) R.gW3[i] = 0.f;
         if (lane == 0) R.gb3 = 0.f;
+        if constexpr (C::EXTRA > 0) {
+            for (int i = lane; i < C::EXTRA * H1; i += 32) R.gX1[i] = 0.f;
+            if constexpr (C::TWO)
+                for (int i = lane; i < C::EXTRA * H2; i += 32) R.gX2[i] = 0.f;
+        }
         __syncwarp();
         for (int t0 = wid * 32; t0 < cnt; t0 += A::T) {
             const int nt = min(32, cnt - t0);
@@ -567,9 +659,14 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll 1
             for (int ch = 0; ch < (C::TWO ? C::NCH : 1); ++ch) {
                 constexpr int NE = KCH <= 16 ? 16 : 32;  // values reduce-scattered
-                float e3[NE];
+                constexpr int NX = C::TWO && C::EXTRA > 0 ? C::EXTRA : 1;
+                float e3[NE], ex[NX][NE];  // W3-bar terms; layer-2 activation-parameter terms
 #pragma unroll
-                for (int k = 0; k < NE; ++k) e3[k] = 0.f;
+                for (int k = 0; k < NE; ++k) {
+                    e3[k] = 0.f;
+#pragma unroll
+                    for (int x = 0; x < NX; ++x) ex[x][k] = 0.f;
+                }
                 if (act) {
                     if constexpr (C::TWO) {
                         float* zrow = &R.zb[lane * A::ZS];
@@ -578,8 +675,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                         for (int k = 0; k < C::KC; ++k) {
                             const int kk = ch * C::KC + k;
-                            float g[J], a, tp, tpp;
-                            tanh_jet<C>(acc[k], g, a, tp, tpp);
+                            const float ck = act_c<C, true>(S, kk), ok = act_o<C, true>(S, kk);
+                            float g[J], a, tp, tpp, tppp;
+                            tanh_jet<C>(acc[k], g, a, tp, tpp, tppp, ck, ok);
                             float gb[J];
                             const float w3 = S.W3[kk];
                             float s3 = 0.f;
@@ -589,8 +687,14 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                 gb[c] = w3 * ob[c];
                             }
                             e3[k] = s3;
-                            float zb[J];
-                            tanh_jet_adj<C>(acc[k], a, tp, tpp, gb, zb);
+                            float zb[J], tpb, tppb;
+                            tanh_jet_adj<C>(acc[k], tp, tpp, tppp, gb, zb, tpb, tppb);
+                            if constexpr (C::EXTRA > 0) {
+                                float pg[C::EXTRA];
+                                act_param_grad<C::ACT>(gb[0], tpb, tppb, acc[k][0], a, tp, tpp, tppp, ck, ok, pg);
+#pragma unroll
+                                for (int x = 0; x < C::EXTRA; ++x) ex[x][k] = pg[x];
+                            }
 #pragma unroll
                             for (int c = 0; c < J; ++c) acc[k][c] = zb[c];
                         }
@@ -618,6 +722,17 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                 } else {
                     if (lane < KCH) R.gW3[ch * KCH + lane] += e3[0];
                 }
+                if constexpr (C::TWO && C::EXTRA > 0) {
+#pragma unroll
+                    for (int x = 0; x < C::EXTRA; ++x) {
+                        warp_reduce_scatter<NE>(ex[x], lane);
+                        if constexpr (NE == 16) {
+                            if (!(lane & 1) && (lane >> 1) < KCH) R.gX2[x * H2 + ch * KCH + (lane >> 1)] += ex[x][0];
+                        } else {
+                            if (lane < KCH) R.gX2[x * H2 + ch * KCH + lane] += ex[x][0];
+                        }
+                    }
+                }
             }
             const float ob0 = ob[0];
             float b3 = ob0;
@@ -628,8 +743,10 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             // ---------------- phase B: layer-1 adjoint ----------------
             // per chunk of NC first-layer neurons: v-bar = W2^T z2-bar (own row), the
             // layer-1 jet adjoint, and the W1-bar / b1-bar terms summed over the warp
-            constexpr int NC = 8 < H1 ? 8 : H1;
-            static_assert(NC * (XD + 1) <= 32, "layer-1 chunk must fit one reduce-scatter");
+            constexpr int RN = XD + 1 + C::EXTRA;  // reduced values per neuron: W1-bar row, b1-bar, parameters
+            constexpr int NCF = 32 / RN >= 8 ? 8 : (32 / RN >= 4 ? 4 : 2);
+            constexpr int NC = NCF < H1 ? NCF : H1;
+            static_assert(NC * RN <= 32 && H1 % NC == 0, "layer-1 chunk must fit one reduce-scatter");
 #pragma unroll 1
             for (int n0 = 0; n0 < H1; n0 += NC) {
                 float r1[32];
@@ -673,8 +790,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                     for (int q = 0; q < NC; ++q) {
                         const int n = n0 + q;
-                        float a, tp, tpp;
-                        C::AF::derivs(a1row[n], a, tp, tpp);
+                        const float cn = act_c<C, false>(S, n), on = act_o<C, false>(S, n);
+                        float a, tp, tpp, tppp;
+                        C::AF::derivs(a1row[n], cn, on, a, tp, tpp, tppp);
                         float tpb = 0.f, tppb = 0.f, cwb[XD];
 #pragma unroll
                         for (int d = 0; d < XD; ++d) {
@@ -689,19 +807,28 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             for (int d = 0; d < XD; ++d)
                                 if ((C::slot_dims(s) >> d) & 1) cwb[d] += 2.0f * g * tpp * S.cw[n * XD + d];
                         }
-                        const float z1b = C::AF::zbar0(vb[q][0], tpb, tppb, a, tp, tpp);
+                        const float z1b = vb[q][0] * tp + tpb * tpp + tppb * tppp;
 #pragma unroll
-                        for (int d = 0; d < XD; ++d) r1[q * (XD + 1) + d] = fmaf(z1b, xn[d], cwb[d] * S.inv_sd[d]);
-                        r1[q * (XD + 1) + XD] = z1b;
+                        for (int d = 0; d < XD; ++d) r1[q * RN + d] = fmaf(z1b, xn[d], cwb[d] * S.inv_sd[d]);
+                        r1[q * RN + XD] = z1b;
+                        if constexpr (C::EXTRA > 0) {
+                            // the stored value of an adaptive activation is the pre-activation z
+                            float pg[C::EXTRA];
+                            act_param_grad<C::ACT>(vb[q][0], tpb, tppb, a1row[n], a, tp, tpp, tppp, cn, on, pg);
+#pragma unroll
+                            for (int x = 0; x < C::EXTRA; ++x) r1[q * RN + XD + 1 + x] = pg[x];
+                        }
                     }
                 }
                 warp_reduce_scatter<32>(r1, lane);
-                if (lane < NC * (XD + 1)) {
-                    const int q = lane / (XD + 1), d = lane - q * (XD + 1);
+                if (lane < NC * RN) {
+                    const int q = lane / RN, d = lane - q * RN;
                     if (d < XD)
                         R.gW1[(n0 + q) * XD + d] += r1[0];
-                    else
+                    else if (d == XD)
                         R.gb1[n0 + q] += r1[0];
+                    else if constexpr (C::EXTRA > 0)
+                        R.gX1[(d - XD - 1) * H1 + n0 + q] += r1[0];
                 }
             }
             // ---------------- phase C: W2-bar over the tile ----------------
@@ -725,8 +852,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             float m[A::NB][3];
 #pragma unroll
                             for (int q = 0; q < A::NB; ++q) {
-                                float a, tp, tpp;
-                                C::AF::derivs(R.a1[t * A::AS + n0 + q], a, tp, tpp);
+                                float a, tp, tpp, tppp;
+                                C::AF::derivs(R.a1[t * A::AS + n0 + q], act_c<C, false>(S, n0 + q),
+                                              act_o<C, false>(S, n0 + q), a, tp, tpp, tppp);
                                 m[q][0] = a;
                                 m[q][1] = tp;
                                 m[q][2] = tpp;
@@ -815,6 +943,23 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
             for (int w = 0; w < NW; ++w) v += RW[w].gb3;
             dst[C::ob3] = v;
+        }
+        if constexpr (C::EXTRA > 0) {
+            for (int i = tid; i < C::EXTRA * H1; i += blockDim.x) {
+                float v = 0.f;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) v += RW[w].gX1[i];
+                dst[C::oX1 + i] = v;
+            }
+            if constexpr (C::TWO) {
+                for (int i = tid; i < C::EXTRA * H2; i += blockDim.x) {
+                    float v = 0.f;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) v += RW[w].gX2[i];
+                    dst[C::oX2 + i] = v;
+                }
+            }
+            if (tid < C::EXTRA) dst[C::oX3 + tid] = 0.f;  // the output layer's parameters are unused
         }
     }
 }

@@ -207,8 +207,8 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
                 float av[NA][4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    float a, tp, tpp;
-                    C::AF::derivs(l1_act<C>(S, xn, n4 + q), a, tp, tpp);
+                    float a, tp, tpp, tppp;
+                    C::AF::derivs(l1_act<C>(S, xn, n4 + q), 1.0f, 1.0f, a, tp, tpp, tppp);
                     av[0][q] = a;
                     av[1][q] = tp;
                     if constexpr (NA > 2) av[NA - 1][q] = tpp;
@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
 #pragma unroll
                     for (int c = 0; c < J; ++c) z[c] = acc[c][k];
                     z[0] += S.b2[k];
-                    tanh_jet<C>(z, g, a, tp, tpp);
+                    float tppp;
+                    tanh_jet<C>(z, g, a, tp, tpp, tppp);
                     const float w3 = S.W3[k];
 #pragma unroll
                     for (int c = 0; c < J; ++c) o[c] = fmaf(w3, g[c], o[c]);

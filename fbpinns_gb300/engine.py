@@ -231,12 +231,14 @@ class FBPINNEngine:
         self.layer_sizes = ls
         self.h1 = ls[1]
         self.h2 = ls[2] if len(ls) == 4 else 0
-        self.P = fcn_param_count(ls)
+        self.P = None  # set below from the activation's parameter count
         self.d2mask = int(d2mask)
         if activation not in _lib.ACTIVATIONS:
             raise ValueError(f"activation must be one of {sorted(_lib.ACTIVATIONS)}, not {activation!r}")
         self.activation = activation
         self.act = _lib.ACTIVATIONS[activation]
+        self.extra = _lib.ACT_EXTRA[activation]  # activation parameters per neuron and layer
+        self.P = fcn_param_count(ls, self.extra)
         if not _lib.load().fbp_has_shape(self.xd, self.h1, self.h2, self.d2mask, self.act):
             raise _lib.FBPLibraryError(
                 f"no compiled jet kernels for layer sizes {ls} ({activation}) with second derivatives along dims "

@@ -151,25 +151,29 @@ def unnorm(mu, sd, x):
 # packed parameter layout used by the CUDA kernels
 # ---------------------------------------------------------------------------
 
-def fcn_param_count(layer_sizes):
-    """P = sum over layers of fan_out * (fan_in + 1)."""
-    return sum(fo * (fi + 1) for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]))
+def fcn_param_count(layer_sizes, extra=0):
+    """P = sum over layers of fan_out * (fan_in + 1 + extra): W, b and
+    ``extra`` per-neuron activation parameters (AdaptiveFCN 1, AdaptiveSIREN 2)."""
+    return sum(fo * (fi + 1 + extra) for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]))
 
 
 def pack_layers(layers):
-    """[(W (m,fo,fi), b (m,fo)), ...] -> theta (m, P): per layer W row-major then b."""
+    """[(W (m,fo,fi), b (m,fo), *params (m,fo)), ...] -> theta (m, P): per layer
+    W row-major, b, then the activation parameters in tuple order."""
     m = layers[0][0].shape[0]
-    return torch.cat([t.reshape(m, -1) for w, b in layers for t in (w, b)], dim=1).contiguous()
+    return torch.cat([t.reshape(m, -1) for layer in layers for t in layer], dim=1).contiguous()
 
 
-def unpack_layers(theta, layer_sizes):
-    """theta (m, P) -> [(W, b), ...] as views into theta."""
+def unpack_layers(theta, layer_sizes, extra=0):
+    """theta (m, P) -> [(W, b, *params), ...] as views into theta."""
     out, o = [], 0
     m = theta.shape[0]
     for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
         w = theta[:, o:o + fo * fi].view(m, fo, fi)
         o += fo * fi
-        b = theta[:, o:o + fo]
-        o += fo
-        out.append((w, b))
+        layer = [w]
+        for _ in range(1 + extra):
+            layer.append(theta[:, o:o + fo])
+            o += fo
+        out.append(tuple(layer))
     return out

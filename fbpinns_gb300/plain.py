@@ -56,12 +56,20 @@ class PlainStep:
         mu, sd = (hi + lo) / 2, (hi - lo) / 2
         xn = (xg - mu) / sd
         rows = theta[ids]
-        layers = unpack_layers(rows, eng.layer_sizes)
+        layers = unpack_layers(rows, eng.layer_sizes, eng.extra)
         h = xn
-        act = torch.sin if eng.activation == "sin" else torch.tanh
-        for w, b in layers[:-1]:
-            h = act(torch.baddbmm(b[:, None, :], h, w.transpose(1, 2)))
-        w, b = layers[-1]
+        for layer in layers[:-1]:
+            z = torch.baddbmm(layer[1][:, None, :], h, layer[0].transpose(1, 2))
+            if eng.activation == "tanh":
+                h = torch.tanh(z)
+            elif eng.activation == "sin":
+                h = torch.sin(z)
+            elif eng.activation == "adaptive_tanh":  # a tanh(z / a)
+                a = layer[2][:, None, :]
+                h = a * torch.tanh(z / a)
+            else:  # c sin(o z)
+                h = layer[2][:, None, :] * torch.sin(layer[3][:, None, :] * z)
+        w, b = layers[-1][:2]
         u = torch.baddbmm(b[:, None, :], h, w.transpose(1, 2))
         un = g.unnorms[ids]
         u = u * un[:, None, 1:2] + un[:, None, 0:1]

@@ -24,10 +24,10 @@ import torch
 
 from . import _lib
 from .engine import FBPINNEngine, FBPINNJet, constrained_jets, d2mask_of, jet_index
-from .networks import fcn_param_count, pack_layers, unpack_layers, FCN, SIREN
+from .networks import fcn_param_count, pack_layers, unpack_layers, FCN, SIREN, AdaptiveFCN, AdaptiveSIREN
 
 # network classes with compiled jet kernels, by hidden-layer activation
-NETWORK_ACTIVATIONS = {FCN: "tanh", SIREN: "sin"}
+NETWORK_ACTIVATIONS = {FCN: "tanh", SIREN: "sin", AdaptiveFCN: "adaptive_tanh", AdaptiveSIREN: "adaptive_sin"}
 from .optim import adam_update
 from .takes import get_inputs, split_takes, inside_models, grid_of  # noqa: F401  (re-exported API)
 
@@ -253,7 +253,8 @@ class FBPINNTrainer:
         assert all_params["static"]["domain"]["xd"] == all_params["static"]["problem"]["dims"][1] == xd
         logger.info(f"Total number of subdomains: {m}")
         if c.network not in NETWORK_ACTIVATIONS:
-            raise NotImplementedError("the compiled jet kernels implement the FCN and SIREN networks")
+            raise NotImplementedError("the compiled jet kernels implement the FCN, SIREN, AdaptiveFCN and "
+                                      "AdaptiveSIREN networks")
         activation = NETWORK_ACTIVATIONS[c.network]
         net_static, net_tr = init_subdomain_networks(c.network, c.network_init_kwargs, m, c.seed)
         layer_sizes = list(c.network_init_kwargs["layer_sizes"])
@@ -368,7 +369,7 @@ class FBPINNTrainer:
             torch.cuda.synchronize()
             step.check()
         all_params["trainable"]["network"] = {"subdomain": {"layers": [
-            (w.detach().cpu().clone(), b.detach().cpu().clone()) for w, b in unpack_layers(eng.theta, layer_sizes)]}}
+            tuple(t.detach().cpu().clone() for t in layer) for layer in unpack_layers(eng.theta, layer_sizes, eng.extra)]}}
         if net_static:
             all_params["static"]["network"] = {"subdomain": net_static}
         logger.info(f"[i: {c.n_steps}/{c.n_steps}] Training complete")
@@ -389,9 +390,9 @@ class FBPINNTrainer:
         """(i, all_params, all_opt_states, active, u_test_losses) as numpy, the
         layout of the reference's model pickles (fbpinns/trainers.py:721)."""
         ls = list(self.c.network_init_kwargs["layer_sizes"])
-        layers = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.theta, ls)]
-        mu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m1, ls)]
-        nu = [(w.cpu().numpy().copy(), b.cpu().numpy().copy()) for w, b in unpack_layers(eng.m2, ls)]
+        def tree(t):
+            return [tuple(x.cpu().numpy().copy() for x in layer) for layer in unpack_layers(t, ls, eng.extra)]
+        layers, mu, nu = tree(eng.theta), tree(eng.m1), tree(eng.m2)
         ap = {"static": self._numpy_tree(all_params["static"]),
               "trainable": {"network": {"subdomain": {"layers": layers}},
                             **{k: self._numpy_tree(v) for k, v in all_params["trainable"].items() if k != "network"}}}

@@ -60,8 +60,10 @@ extern "C" {
 #define FBP_D2_GROUP(dims) (((dims) & 7) << 4)
 
 /* Hidden-layer activations of the compiled networks (fbp_net.act). */
-#define FBP_ACT_TANH 0   /* FCN (fbpinns/networks.py:61-68) */
-#define FBP_ACT_SIN 1    /* SIREN (fbpinns/networks.py:102-131) */
+#define FBP_ACT_TANH 0           /* FCN (fbpinns/networks.py:61-68) */
+#define FBP_ACT_SIN 1            /* SIREN (fbpinns/networks.py:102-131) */
+#define FBP_ACT_ADAPTIVE_TANH 2  /* AdaptiveFCN a tanh(z/a) (networks.py:70-100); layers (W, b, a) */
+#define FBP_ACT_ADAPTIVE_SIN 3   /* AdaptiveSIREN c sin(o z) (networks.py:133-163); layers (W, b, c, o) */
 
 /* Device status word bits (written by kernels into an int32 the caller owns). */
 #define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */
@@ -109,9 +111,11 @@ typedef struct fbp_net {
     int32_t d2mask;       /* dims with a pure second-derivative jet */
     int32_t nparam;       /* P: parameters per subdomain (packed layout below) */
     int32_t act;          /* hidden-layer activation, FBP_ACT_* */
-    /* theta (m, P): for each layer in order, W (fan_out, fan_in) row-major
-     * then b (fan_out) — the reference's FCN / SIREN (w, b) list flattened
-     * (fbpinns/networks.py:43-68, 102-131). */
+    /* theta (m, P): for each layer in order, W (fan_out, fan_in) row-major,
+     * b (fan_out), then the layer's activation parameters (fan_out each: a
+     * for FBP_ACT_ADAPTIVE_TANH, c then o for FBP_ACT_ADAPTIVE_SIN; the
+     * output layer's are unused) — the reference's per-layer parameter tuples
+     * flattened (fbpinns/networks.py:43-194). */
     const float* theta;
     const float* xmins;   /* (m, xd) subdomain boxes (norm + window) */
     const float* xmaxs;   /* (m, xd) */

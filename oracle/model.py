@@ -103,13 +103,24 @@ def cosine_window(xmin, xmax, x):
 
 
 def fcn(layers, x, activation="tanh"):
-    """``fbpinns/networks.py:61-68`` (FCN, tanh) and ``:102-131`` (SIREN, sin),
-    batched over pairs: W (s,fo,fi), b (s,fo)."""
-    act = {"tanh": torch.tanh, "sin": torch.sin}[activation]
-    for w, b in layers[:-1]:
+    """The reference's networks batched over pairs: W (s,fo,fi), b (s,fo) and the
+    layer's activation parameters (s,fo): FCN tanh (``fbpinns/networks.py:61-68``),
+    SIREN sin (``:102-131``), AdaptiveFCN a tanh(x/a) (``:70-100``), AdaptiveSIREN
+    c sin(o x) (``:133-163``)."""
+    for layer in layers[:-1]:
+        w, b = layer[0], layer[1]
         x = torch.einsum("sij,sj->si", w, x) + b
-        x = act(x)
-    w, b = layers[-1]
+        if activation == "tanh":
+            x = torch.tanh(x)
+        elif activation == "sin":
+            x = torch.sin(x)
+        elif activation == "adaptive_tanh":
+            x = layer[2] * torch.tanh(x / layer[2])
+        elif activation == "adaptive_sin":
+            x = layer[2] * torch.sin(layer[3] * x)
+        else:
+            raise ValueError(activation)
+    w, b = layers[-1][0], layers[-1][1]
     return torch.einsum("sij,sj->si", w, x) + b
 
 
@@ -135,7 +146,7 @@ def fbpinn_model(P, x_batch, takes, constraining_fn):
     # norm_fn  (decompositions.py:184-188)
     x_norm = norm((xmax + xmin) / 2, (xmax - xmin) / 2, x_take)
     # network_fn  (networks.py:61-68)
-    layers = [(w[m_take], b[m_take]) for w, b in P["layers"]]
+    layers = [tuple(t[m_take] for t in layer) for layer in P["layers"]]
     u_raw = fcn(layers, x_norm, P.get("activation", "tanh"))
     # unnorm_fn  (decompositions.py:191-194)
     un = P["unnorms"][m_take]
@@ -232,7 +243,7 @@ def cut_params(P, ims):
     Q = dict(P)
     for k in ("xmins", "xmaxs", "flags", "unnorms", "pou"):
         Q[k] = P[k][ims]
-    Q["layers"] = [(w[ims], b[ims]) for w, b in P["layers"]]
+    Q["layers"] = [tuple(t[ims] for t in layer) for layer in P["layers"]]
     return Q
 
 
@@ -260,11 +271,12 @@ def value_and_grad(P_all, active_ims, fixed_ims, constraints, takess, jmapss, pr
     na = len(active_ims)
     leaves = []
     layers = []
-    for w, b in Q["layers"]:
-        wa = w[:na].detach().clone().requires_grad_(True)
-        ba = b[:na].detach().clone().requires_grad_(True)
-        leaves += [wa, ba]
-        layers.append((torch.cat([wa, w[na:].detach()]), torch.cat([ba, b[na:].detach()])))
+    sizes = []
+    for layer in Q["layers"]:
+        act_t = [t[:na].detach().clone().requires_grad_(True) for t in layer]
+        leaves += act_t
+        sizes.append(len(layer))
+        layers.append(tuple(torch.cat([ta, t[na:].detach()]) for ta, t in zip(act_t, layer)))
     Q["layers"] = layers
     pt = {}
     for k in trainable_problem_keys:
@@ -274,9 +286,11 @@ def value_and_grad(P_all, active_ims, fixed_ims, constraints, takess, jmapss, pr
     loss = fbpinn_loss(Q, constraints, takess, jmapss, problem)
     g = torch.autograd.grad(loss, leaves, allow_unused=True)
     g = [torch.zeros_like(l) if gi is None else gi for gi, l in zip(g, leaves)]
-    nl = len(Q["layers"])
-    grads = [(g[2 * i], g[2 * i + 1]) for i in range(nl)]
-    gprob = {k: g[2 * nl + j] for j, k in enumerate(trainable_problem_keys)}
+    grads, o = [], 0
+    for k in sizes:
+        grads.append(tuple(g[o:o + k]))
+        o += k
+    gprob = {k: g[o + j] for j, k in enumerate(trainable_problem_keys)}
     return loss.detach(), grads, gprob
 
 

@@ -217,7 +217,11 @@ def main():
         layers = []
         for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
             v = wscale * np.sqrt(1 / fi)
-            layers.append((jnp.array(r.uniform(-v, v, (m, fo, fi))), jnp.array(r.uniform(-v, v, (m, fo)))))
+            layer = (jnp.array(r.uniform(-v, v, (m, fo, fi))), jnp.array(r.uniform(-v, v, (m, fo))))
+            # adaptive activations: per-neuron parameters away from their initial 1
+            nx = {"AdaptiveFCN": 1, "AdaptiveSIREN": 2}.get(network, 0)
+            layer += tuple(jnp.array(r.uniform(0.5, 1.5, (m, fo))) for _ in range(nx))
+            layers.append(layer)
         sub = sp_params["subdomain"]["params"]
         keep = far_from_edges(xb, np.asarray(sub[0]), np.asarray(sub[1]), 1e-2)
         xb = xb[keep].astype(np.float64)
@@ -238,9 +242,11 @@ def main():
         arrays = dict(x_batch=xb, m_take=takes[0], n_take=takes[1], p_take=takes[2], np_take=takes[3],
                       npou=takes[4], all_ims=all_ims, u=u, wp=wp, us=us, ws=ws, us_raw=ur,
                       u_raw=ufun_raw(xb))
-        for i, (W, b) in enumerate(layers):
-            arrays[f"W{i}"] = W
-            arrays[f"b{i}"] = b
+        for i, layer in enumerate(layers):
+            arrays[f"W{i}"] = layer[0]
+            arrays[f"b{i}"] = layer[1]
+            for k, t in zip("AO", layer[2:]):  # AdaptiveFCN: a; AdaptiveSIREN: c, o
+                arrays[f"{k}{i}"] = t
         for k, v in jets.items():
             arrays["d" + "".join(map(str, k))] = v
         for k, v in jets_raw.items():
@@ -279,6 +285,20 @@ def main():
     loss_fns["multilevel_siren"] = loss_fns["multilevel"]
     model_case("multilevel_siren", DM, spm, BU, dict(), [2, 8, 8, 1], rng_s.uniform(0, 1, (600, 2)), 16, [0, 1],
                network="SIREN", wscale=np.sqrt(6.0))
+    # AdaptiveFCN (networks.py:70-100) and AdaptiveSIREN (networks.py:133-163)
+    rng_a = np.random.default_rng(37)
+    loss_fns["ho_hardbc_adafcn"] = loss_fns["ho_hardbc"]
+    model_case("ho_hardbc_adafcn", D, sp, HOH, dict(d=2, w0=80, sd=0.1), [1, 8, 8, 1], xho, 17, [0],
+               network="AdaptiveFCN")
+    loss_fns["multilevel_adafcn"] = loss_fns["multilevel"]
+    model_case("multilevel_adafcn", DM, spm, BU, dict(), [2, 8, 8, 1], rng_a.uniform(0, 1, (600, 2)), 18, [0, 1],
+               network="AdaptiveFCN")
+    loss_fns["ho_hardbc_adasiren"] = loss_fns["ho_hardbc"]
+    model_case("ho_hardbc_adasiren", D, sp, HOH, dict(d=2, w0=80, sd=0.1), [1, 8, 8, 1], xho, 19, [0],
+               network="AdaptiveSIREN", wscale=np.sqrt(6.0))
+    loss_fns["multilevel_adasiren"] = loss_fns["multilevel"]
+    model_case("multilevel_adasiren", DM, spm, BU, dict(), [2, 8, 8, 1], rng_a.uniform(0, 1, (600, 2)), 20,
+               [0, 1], network="AdaptiveSIREN", wscale=np.sqrt(6.0))
 
     # constraining functions and losses on given jets
     xc = rng.uniform([-1, -1, 0], [1, 1, 1], (64, 3))

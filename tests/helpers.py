@@ -44,22 +44,38 @@ def boxes_static(xmin, xmax, pou=None):
 
 
 def golden_layers(g):
+    """Layer tuples (W, b[, a] or [, c, o]) of a golden model fixture."""
     out, i = [], 0
     while f"W{i}" in g:
-        out.append((torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])))
+        layer = [torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])]
+        layer += [torch.tensor(g[f"{k}{i}"]) for k in "AO" if f"{k}{i}" in g]
+        out.append(tuple(layer))
         i += 1
     return out
 
 
+GOLDEN_ACTIVATION = {"siren": "sin", "adafcn": "adaptive_tanh", "adasiren": "adaptive_sin"}
+
+
+def golden_activation(tag):
+    """Activation of a golden model tag (suffix _siren, _adafcn, _adasiren; else tanh)."""
+    return GOLDEN_ACTIVATION.get(tag.rsplit("_", 1)[-1], "tanh")
+
+
+def golden_base(tag):
+    """The decomposition recipe of a golden model tag."""
+    return tag.rsplit("_", 1)[0] if tag.rsplit("_", 1)[-1] in GOLDEN_ACTIVATION else tag
+
+
 def layer_sizes(layers):
-    return [layers[0][0].shape[2]] + [w.shape[1] for w, _ in layers]
+    return [layers[0][0].shape[2]] + [layer[0].shape[1] for layer in layers]
 
 
 def oracle_params(static, layers64, problem=None):
     """Oracle parameter dict (float64) from the product static params."""
     p = static["subdomain"]["params"]
     P = {"xmins": p[0].double(), "xmaxs": p[1].double(), "flags": p[4].double(), "unnorms": p[5].double(),
-         "pou": static["subdomain"]["pou"].double(), "layers": [(w.double(), b.double()) for w, b in layers64],
+         "pou": static["subdomain"]["pou"].double(), "layers": [tuple(t.double() for t in l) for l in layers64],
          "problem": problem or {}, "problem_trainable": {}}
     return P
 

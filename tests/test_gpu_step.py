@@ -13,7 +13,8 @@ import pytest
 import torch
 
 from conftest import golden
-from helpers import decomposition, golden_layers, layer_sizes, oracle_params, rel_err, random_layers
+from helpers import (decomposition, golden_activation, golden_base, golden_layers, layer_sizes, oracle_params,
+                     rel_err, random_layers)
 from oracle import model as OM
 from oracle import problems as OP
 from oracle import takes as OT
@@ -30,20 +31,23 @@ GRAD_TOL = 1e-4
 
 def _engine(static, layers, d2mask, chunk=64, activation="tanh"):
     eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk, activation=activation)
-    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
     return eng
 
 
 @pytest.mark.parametrize("tag,dims,d2", [("ho_hardbc", [0], 1), ("burgers", [0, 1], 1), ("wave", [0, 1, 2], 7),
                                          ("multilevel", [0, 1], 3), ("ho_hardbc_siren", [0], 1),
-                                         ("multilevel_siren", [0, 1], 3)])
+                                         ("multilevel_siren", [0, 1], 3), ("ho_hardbc_adafcn", [0], 1),
+                                         ("multilevel_adafcn", [0, 1], 3), ("ho_hardbc_adasiren", [0], 1),
+                                         ("multilevel_adasiren", [0, 1], 3)])
 def test_jets_vs_reference_golden(cuda, tag, dims, d2):
     """POU-combined network jets (before the constraint) vs the reference's
-    forward values and their float64 finite differences (FCN and SIREN)."""
+    forward values and their float64 finite differences (FCN, SIREN,
+    AdaptiveFCN, AdaptiveSIREN)."""
     g = golden(f"model_{tag}.npz")
-    static = decomposition(tag.replace("_siren", ""))
+    static = decomposition(golden_base(tag))
     layers = golden_layers(g)
-    eng = _engine(static, layers, d2, activation="sin" if tag.endswith("_siren") else "tanh")
+    eng = _engine(static, layers, d2, activation=golden_activation(tag))
     ps = eng.points(torch.tensor(g["x_batch"], dtype=torch.float32))
     U = FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy()
     xd = len(static["subdomain"]["params"][0][0])
@@ -132,26 +136,33 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     assert np.all(grad[inactive] == 0)
 
 
+@pytest.mark.parametrize("act", ["sin", "adaptive_tanh", "adaptive_sin"])
 @pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("poisson", False), ("poisson", True)])
-def test_siren_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
-    """SIREN networks (sin activations, U(+-sqrt(6/fan_in)) weights): fused loss
-    and per-subdomain gradients vs the float64 oracle."""
+def test_network_fused_loss_and_gradient_vs_oracle(cuda, name, lap, act):
+    """SIREN, AdaptiveFCN and AdaptiveSIREN networks (adaptive parameters drawn
+    away from 1): fused loss and per-subdomain gradients -- W, b and the
+    activation parameters -- vs the float64 oracle."""
     recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
     ls = [ls[0], 8, 8, 1]
     static = decomposition(recipe)
-    layers64 = [(w * math.sqrt(6.0), b * math.sqrt(6.0)) for w, b in random_layers(ls, static["m"], seed=7)]
-    layers32 = [(w.float().double(), b.float().double()) for w, b in layers64]
+    scale = 1.0 if act == "adaptive_tanh" else math.sqrt(6.0)
+    gen = torch.Generator().manual_seed(71)
+    nx = {"sin": 0, "adaptive_tanh": 1, "adaptive_sin": 2}[act]
+    layers64 = [(w * scale, b * scale) + tuple(0.5 + torch.rand(b.shape, generator=gen, dtype=torch.float64)
+                                               for _ in range(nx))
+                for w, b in random_layers(ls, static["m"], seed=7)]
+    layers32 = [tuple(t.float().double() for t in layer) for layer in layers64]
     x = _points(recipe if recipe != "multilevel" else "poisson", 500, 23)
     prob_static = pcls.init_params(**pkw)[0]
     P = oracle_params(static, layers32, opar)
-    P["activation"] = "sin"
+    P["activation"] = act
     p = static["subdomain"]["params"]
     takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(static["m"], dtype=int), p[0].numpy(),
                                                           p[1].numpy(), static["subdomain"]["pou"].numpy())
     loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
                                            [OM.get_jmaps(_required(name))], ocls)
-    g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
-    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0), activation="sin")
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for layer in grads for t in layer], 1).numpy()
+    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0), activation=act)
     assert not eng.tensor_cores
     eng.set_state(active)
     eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))

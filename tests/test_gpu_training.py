@@ -91,3 +91,21 @@ def test_siren_network_trains_fused(cuda):
     assert tr.engine.activation == "sin" and not tr.engine.tensor_cores
     losses = [h["loss"] for h in tr.history]
     assert all(math.isfinite(v) for v in losses) and losses[-1] < losses[0]
+
+
+@pytest.mark.parametrize("netname", ["AdaptiveFCN", "AdaptiveSIREN"])
+def test_adaptive_networks_train_fused(cuda, netname):
+    """Adaptive networks through the fused engine: the HO problem trains, the
+    activation parameters move, and the returned params keep the reference's
+    per-layer tuples (W, b, a) / (W, b, c, o)."""
+    from fbpinns_gb300 import networks
+    c = configs.ho(n_steps=150)
+    c.network = getattr(networks, netname)
+    c.summary_freq, c.test_freq = 50, 150
+    tr = FBPINNTrainer(c)
+    ap = tr.train()
+    losses = [h["loss"] for h in tr.history]
+    assert all(math.isfinite(v) for v in losses) and losses[-1] < losses[0]
+    layers = ap["trainable"]["network"]["subdomain"]["layers"]
+    assert all(len(layer) == (3 if netname == "AdaptiveFCN" else 4) for layer in layers)
+    assert not torch.allclose(layers[0][2], torch.ones_like(layers[0][2]))

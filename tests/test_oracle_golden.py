@@ -6,6 +6,7 @@ import pytest
 import torch
 
 from conftest import golden
+from helpers import golden_activation, golden_base, golden_layers
 from oracle import takes as OT
 from oracle import model as OM
 from oracle import problems as OP
@@ -95,15 +96,11 @@ def test_level_params_match_reference(name, recipe):
 
 
 def _oracle_params(g, tag, decomp):
-    ps_full = _level_full(tag.replace("_siren", ""))
+    ps_full = _level_full(golden_base(tag))
     P = {"xmins": torch.tensor(ps_full[0]), "xmaxs": torch.tensor(ps_full[1]),
          "flags": torch.tensor(ps_full[4]), "unnorms": torch.tensor(ps_full[5]),
-         "pou": torch.tensor(ps_full[6]), "layers": [],
-         "activation": "sin" if tag.endswith("_siren") else "tanh"}
-    i = 0
-    while f"W{i}" in g:
-        P["layers"].append((torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])))
-        i += 1
+         "pou": torch.tensor(ps_full[6]), "layers": golden_layers(g),
+         "activation": golden_activation(tag)}
     return P
 
 
@@ -131,11 +128,13 @@ PROBLEMS = {
              [0, 1, 2]),
     "multilevel": (OP.BurgersEquation2D, {"sd": 0.1, "nu": 0.01 / np.pi}, [0, 1]),
 }
-PROBLEMS["ho_hardbc_siren"] = PROBLEMS["ho_hardbc"]  # SIREN networks (networks.py:102-131)
-PROBLEMS["multilevel_siren"] = PROBLEMS["multilevel"]
+for _net in ("siren", "adafcn", "adasiren"):  # SIREN, AdaptiveFCN, AdaptiveSIREN (networks.py:70-163)
+    PROBLEMS[f"ho_hardbc_{_net}"] = PROBLEMS["ho_hardbc"]
+    PROBLEMS[f"multilevel_{_net}"] = PROBLEMS["multilevel"]
+NET_TAGS = [f"{b}_{n}" for n in ("siren", "adafcn", "adasiren") for b in ("ho_hardbc", "multilevel")]
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel", "ho_hardbc_siren", "multilevel_siren"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel"] + NET_TAGS)
 def test_model_forward_matches_reference(tag):
     """oracle FBPINN_model (float64) == the reference's FBPINN_model run on numpy."""
     g = golden(f"model_{tag}.npz")
@@ -153,7 +152,7 @@ def test_model_forward_matches_reference(tag):
     np.testing.assert_allclose(ur.numpy(), g["us_raw"], rtol=1e-10, atol=1e-12)
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel", "ho_hardbc_siren", "multilevel_siren"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel"] + NET_TAGS)
 def test_model_jets_match_reference_fd(tag):
     """oracle nested-jvp jets == float64 finite differences of the reference model."""
     g = golden(f"model_{tag}.npz")
@@ -172,7 +171,8 @@ def test_model_jets_match_reference_fd(tag):
             assert err < 2e-6, (nm, err)
 
 
-@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "ho_hardbc_siren"])
+@pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "ho_hardbc_siren", "ho_hardbc_adafcn",
+                                 "ho_hardbc_adasiren"])
 def test_loss_matches_reference(tag):
     g = golden(f"model_{tag}.npz")
     prob, pp, dims = PROBLEMS[tag]
@@ -181,6 +181,8 @@ def test_loss_matches_reference(tag):
     takes = (g["m_take"], g["n_take"], g["p_take"], g["np_take"], int(g["npou"]))
     x = torch.tensor(g["x_batch"])
     req = {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))), "ho_hardbc_siren": ((0, ()), (0, (0,)), (0, (0, 0))),
+           "ho_hardbc_adafcn": ((0, ()), (0, (0,)), (0, (0, 0))),
+           "ho_hardbc_adasiren": ((0, ()), (0, (0,)), (0, (0, 0))),
            "burgers": ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0))),
            "wave": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2)))}[tag]
     loss = OM.fbpinn_loss(P, [[x]], [takes], [OM.get_jmaps(req)], prob)
