@@ -36,6 +36,10 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 constexpr int kSM = 152;  // GB300 SM count (grid sizing hint; queried at run time too)
 
+// Per-device caches (kernel attributes, occupancy-sized grids) are indexed by
+// the current device, 0 .. FBP_MAX_DEVICES - 1.
+constexpr int FBP_MAX_DEVICES = 64;
+int current_device();
 int sm_count();
 
 __host__ __device__ constexpr int popc_const(int v) {

@@ -20,10 +20,11 @@ int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, floa
                    cudaStream_t st) {
     using C = Cfg<XD, H1, H2, D2, ACT>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward: nparam %d != %d for this shape", net.nparam, C::P);
-    static int auto_grid = 0;
+    static int auto_grid[FBP_MAX_DEVICES] = {};
+    const int dev = current_device();
     if (grid <= 0) {
-        if (!auto_grid) auto_grid = resident_grid(forward_pairs_kernel<C>, FWD_THREADS, 0);
-        grid = auto_grid;
+        if (!auto_grid[dev]) auto_grid[dev] = resident_grid(forward_pairs_kernel<C>, FWD_THREADS, 0);
+        grid = auto_grid[dev];
     }
     forward_pairs_kernel<C><<<grid, FWD_THREADS, 0, st>>>(net, x, pr, pair_out);
     FBP_LAUNCH_CHECK();
@@ -36,15 +37,16 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
     using C = Cfg<XD, H1, H2, D2, ACT>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "adjoint: nparam %d != %d for this shape", net.nparam, C::P);
     const size_t shm = sizeof(WarpRows<C>) * AdjW<C>::W;
-    static bool attr_set = false;
-    static int auto_grid = 0;
-    if (!attr_set) {
+    static bool attr_set[FBP_MAX_DEVICES] = {};
+    static int auto_grid[FBP_MAX_DEVICES] = {};
+    const int dev = current_device();
+    if (!attr_set[dev]) {
         FBP_CUDA_CHECK(cudaFuncSetAttribute(adjoint_pairs_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-        attr_set = true;
+        attr_set[dev] = true;
     }
     if (grid <= 0) {
-        if (!auto_grid) auto_grid = resident_grid(adjoint_pairs_kernel<C>, AdjW<C>::T, shm);
-        grid = auto_grid;
+        if (!auto_grid[dev]) auto_grid[dev] = resident_grid(adjoint_pairs_kernel<C>, AdjW<C>::T, shm);
+        grid = auto_grid[dev];
     }
     adjoint_pairs_kernel<C><<<grid, AdjW<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
     FBP_LAUNCH_CHECK();

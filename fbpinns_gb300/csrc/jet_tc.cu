@@ -12,7 +12,9 @@ static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs
     using C = Cfg<XD, 16, 16, D2>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward_tc: nparam %d != %d for this shape", net.nparam, C::P);
     const size_t shm = sizeof(TcSmem<C>);
-    static int res = 0;
+    static int res_dev[FBP_MAX_DEVICES] = {};  // per device
+    const int dev = current_device();
+    int& res = res_dev[dev];
     if (!res) {
         FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)shm));
@@ -20,8 +22,7 @@ static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs
         // upper bound on how many can be resident at once
         cudaFuncAttributes fa;
         FBP_CUDA_CHECK(cudaFuncGetAttributes(&fa, forward_pairs_tc_kernel<C>));
-        int dev = 0, smem_sm = 0, regs_sm = 0, thr_sm = 0;
-        FBP_CUDA_CHECK(cudaGetDevice(&dev));
+        int smem_sm = 0, regs_sm = 0, thr_sm = 0;
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));

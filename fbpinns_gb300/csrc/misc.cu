@@ -17,16 +17,22 @@ void set_error(const char* fmt, ...) {
     va_end(ap);
 }
 
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= FBP_MAX_DEVICES) dev = 0;
+    return dev;
+}
+
 int sm_count() {
-    static int cached = 0;
-    if (cached) return cached;
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
-        cached = n;
+    static int cached[FBP_MAX_DEVICES] = {};  // per device
+    const int dev = current_device();
+    if (cached[dev]) return cached[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
+        cached[dev] = n;
     else
-        cached = kSM;
-    return cached;
+        cached[dev] = kSM;
+    return cached[dev];
 }
 
 // ---------------------------------------------------------------------------

@@ -120,10 +120,16 @@ class FusedStep:
     fixed-capacity buffers (``headroom`` x the first batch's sizes), so the step
     has no host synchronisation and is captured in one CUDA graph when
     ``use_graph``.
+
+    With ``resample`` the next step's points depend only on the step count, so
+    (``pipeline``, default) two point sets alternate: while step t trains on
+    one, a second stream draws step t+1's points and builds their lists into
+    the other (stream offset = the count at step t's start + 1, the offset
+    step t+1 would use).  The results are bit-identical to the serial step.
     """
 
     def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
-                 headroom=1.25):
+                 headroom=1.25, pipeline=True):
         self.eng, self.opt = engine, opt
         engine.set_problem(spec)
         self.resample = resample
@@ -147,11 +153,45 @@ class FusedStep:
         else:
             self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(dev))
         self.loss_host = torch.zeros(1, dtype=torch.float64, pin_memory=True)
+        self.pipeline = bool(pipeline) and resample is not None
+        if self.pipeline:
+            self.sets = [self.ps, engine.points(self.ps.x.clone(), caps=caps)]
+            self.cur = 0
+            self.snap = torch.zeros(1, dtype=torch.int32, device=dev)  # count at the step's start
+            # higher priority: the list kernels take SMs ahead of the persistent adjoint's CTAs
+            self.side = torch.cuda.Stream(device=dev, priority=-1)
+            self.graphs = [None, None]
+            self._prologue()
+
+    def _prologue(self):
+        """The current point set's points and lists for the current step count."""
+        ps = self.sets[self.cur]
+        self.eng.sample(ps.x, self.seed, 0, self.xmin, self.xmax, counter=self.eng.count)
+        ps.rebuild()
+        self.ps = ps
 
     def set_state(self, active):
         self.eng.set_state(active)
-        self.ps.build_work()
+        for ps in (self.sets if self.pipeline else [self.ps]):
+            ps.build_work()
         self.graph = None
+        if self.pipeline:
+            self.graphs = [None, None]
+
+    def _body_pipelined(self, cur):
+        """Step on point set cur while the other set is rebuilt for the next step."""
+        eng, o = self.eng, self.opt
+        main = torch.cuda.current_stream()
+        a, b = self.sets[cur], self.sets[1 - cur]
+        self.snap.copy_(eng.count)
+        with torch.cuda.stream(self.side):
+            self.side.wait_stream(main)
+            eng.sample(b.x, self.seed, 1, self.xmin, self.xmax, counter=self.snap, stream=self.side)
+            b.rebuild(stream=self.side)
+        loss = eng.fused_step(a, o["learning_rate"], stream=main, b1=o["b1"], b2=o["b2"], eps=o["eps"],
+                              eps_root=o["eps_root"])
+        main.wait_stream(self.side)
+        return loss
 
     def _body(self, stream=None):
         eng, o = self.eng, self.opt
@@ -164,20 +204,33 @@ class FusedStep:
                               eps_root=o["eps_root"])
 
     def capture(self, warmup=2):
-        """Capture one step in a CUDA graph after ``warmup`` eager steps on a side
-        stream; the warm-up steps' updates (parameters, Adam moments, step count,
-        hence also the sampler's stream offset) are rolled back, so capturing does
-        not advance training."""
+        """Capture the step in a CUDA graph (one per point set when pipelined)
+        after ``warmup`` eager steps on a side stream; the warm-up steps'
+        updates (parameters, Adam moments, step count, hence also the sampler's
+        stream offset) are rolled back, so capturing does not advance training."""
         eng = self.eng
         saved = [t.clone() for t in (eng.theta, eng.m1, eng.m2, eng.count)]
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
-            for _ in range(warmup):
-                self._body()
+            for w in range(warmup):
+                if self.pipeline:
+                    self._body_pipelined(w % 2)
+                else:
+                    self._body()
         torch.cuda.current_stream().wait_stream(s)
         for dst, src in zip((eng.theta, eng.m1, eng.m2, eng.count), saved):
             dst.copy_(src)
+        if self.pipeline:
+            for cur in (0, 1):
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._body_pipelined(cur)
+                self.graphs[cur] = g
+            self.cur = 0
+            self._prologue()  # the current set again, for the rolled-back count
+            self.graph = self.graphs
+            return
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self._body()
@@ -189,7 +242,16 @@ class FusedStep:
         copied back to ``loss_host`` (read it after a synchronisation)."""
         if self.host:
             self.ps.x.copy_(x_host, non_blocking=True)
-        if self.use_graph:
+        if self.pipeline:
+            if self.use_graph:
+                if self.graph is None:
+                    self.capture()
+                self.graphs[self.cur].replay()
+            else:
+                self._body_pipelined(self.cur)
+            self.cur = 1 - self.cur
+            self.ps = self.sets[self.cur]  # holds the next step's lists
+        elif self.use_graph:
             if self.graph is None:
                 self.capture()
             self.graph.replay()
@@ -200,7 +262,8 @@ class FusedStep:
         return self.eng.loss
 
     def check(self):
-        self.ps.check_status()
+        for ps in (self.sets if self.pipeline else [self.ps]):
+            ps.check_status()
 
 
 def init_subdomain_networks(network, kwargs, m, seed):

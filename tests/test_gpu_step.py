@@ -358,6 +358,32 @@ def test_resampled_graph_step_is_deterministic_and_matches_eager(cuda):
     assert torch.equal(t_g, t_e)
 
 
+def test_pipelined_resampling_matches_serial_steps(cuda):
+    """Building the next step's lists on a second stream while the current step
+    trains (two point sets, two graphs) gives bit-identical parameters, loss
+    and step count to the serial resampled step."""
+    from fbpinns_gb300.trainers import FusedStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=2)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    results = []
+    for pipeline, use_graph in ((False, True), (True, True), (True, False)):
+        eng = _engine(static, layers, 3 | _lib.D2_LAPLACIAN, chunk=512)
+        st = FusedStep(eng, spec, adam(1e-3), resample=(1 << 14, [0., 0.], [1., 1.], 5), use_graph=use_graph,
+                       pipeline=pipeline)
+        losses = [st.step().item() for _ in range(5)]
+        torch.cuda.synchronize()
+        st.check()
+        results.append((eng.theta.cpu().clone(), losses, int(eng.count.item())))
+    ref = results[0]
+    for theta, losses, count in results[1:]:
+        assert count == ref[2] == 5
+        assert losses == ref[1]
+        assert torch.equal(theta, ref[0])
+
+
 def test_resampled_steps_match_oracle_points(cuda):
     """The points drawn on the device are uniform in the box and each step's
     interaction lists equal the oracle's for those points."""
