@@ -280,16 +280,18 @@ def run_fused(args, world, rank, local):
         rng = np.random.default_rng(seed + 7)
         nh = 4
         host = [torch.from_numpy(rng.uniform(0, 1, (N_POINTS, 2)).astype(np.float32)).pin_memory() for _ in range(nh)]
-        hstep = FusedStep(eng2, spec, opt, host_points=N_POINTS, x_probe=host[0], use_graph=True)
+        # pipelined: each call copies the next step's points in and builds their lists on a
+        # second stream while the step trains on the current ones
+        hstep = FusedStep(eng2, spec, opt, host_points=N_POINTS, x_probe=host[0], use_graph=True, pipeline=True)
         for k in range(max(args.warmup, 3)):
-            hstep.step(host[k % nh])
+            hstep.step(host[k % nh], host[(k + 1) % nh])
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record()
         for k in range(args.steps):
-            hstep.step(host[k % nh])
+            hstep.step(host[k % nh], host[(k + 1) % nh])
         f1.record()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0

@@ -121,15 +121,17 @@ class FusedStep:
     has no host synchronisation and is captured in one CUDA graph when
     ``use_graph``.
 
-    With ``resample`` the next step's points depend only on the step count, so
-    (``pipeline``, default) two point sets alternate: while step t trains on
-    one, a second stream draws step t+1's points and builds their lists into
-    the other (stream offset = the count at step t's start + 1, the offset
-    step t+1 would use).  The results are bit-identical to the serial step.
+    With ``pipeline`` two point sets alternate: while step t trains on one, a
+    second stream builds step t+1's lists into the other.  With ``resample``
+    (pipelined by default) it also draws step t+1's points (stream offset =
+    the count at step t's start + 1, the offset step t+1 would use); with
+    ``host_points`` (``pipeline=True`` opt-in) the caller passes the next
+    step's points as well, ``step(x_host, x_next)``, and they are copied in
+    before the step.  The results are bit-identical to the serial step.
     """
 
     def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
-                 headroom=1.25, pipeline=True):
+                 headroom=1.25, pipeline=None):
         self.eng, self.opt = engine, opt
         engine.set_problem(spec)
         self.resample = resample
@@ -153,20 +155,25 @@ class FusedStep:
         else:
             self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(dev))
         self.loss_host = torch.zeros(1, dtype=torch.float64, pin_memory=True)
-        self.pipeline = bool(pipeline) and resample is not None
+        if pipeline is None:
+            pipeline = resample is not None
+        self.pipeline = bool(pipeline) and (resample is not None or self.host)
         if self.pipeline:
             self.sets = [self.ps, engine.points(self.ps.x.clone(), caps=caps)]
             self.cur = 0
+            self.started = False
             self.snap = torch.zeros(1, dtype=torch.int32, device=dev)  # count at the step's start
             # higher priority: the list kernels take SMs ahead of the persistent adjoint's CTAs
             self.side = torch.cuda.Stream(device=dev, priority=-1)
             self.graphs = [None, None]
-            self._prologue()
+            if resample is not None:
+                self._prologue()
 
     def _prologue(self):
         """The current point set's points and lists for the current step count."""
         ps = self.sets[self.cur]
-        self.eng.sample(ps.x, self.seed, 0, self.xmin, self.xmax, counter=self.eng.count)
+        if self.resample is not None:
+            self.eng.sample(ps.x, self.seed, 0, self.xmin, self.xmax, counter=self.eng.count)
         ps.rebuild()
         self.ps = ps
 
@@ -186,7 +193,8 @@ class FusedStep:
         self.snap.copy_(eng.count)
         with torch.cuda.stream(self.side):
             self.side.wait_stream(main)
-            eng.sample(b.x, self.seed, 1, self.xmin, self.xmax, counter=self.snap, stream=self.side)
+            if self.resample is not None:
+                eng.sample(b.x, self.seed, 1, self.xmin, self.xmax, counter=self.snap, stream=self.side)
             b.rebuild(stream=self.side)
         loss = eng.fused_step(a, o["learning_rate"], stream=main, b1=o["b1"], b2=o["b2"], eps=o["eps"],
                               eps_root=o["eps_root"])
@@ -227,8 +235,11 @@ class FusedStep:
                 with torch.cuda.graph(g):
                     self._body_pipelined(cur)
                 self.graphs[cur] = g
-            self.cur = 0
-            self._prologue()  # the current set again, for the rolled-back count
+            if self.resample is not None:
+                self.cur = 0
+                self._prologue()  # the current set again, for the rolled-back count
+            else:
+                self.sets[self.cur].rebuild()  # the warm-up rebuilt both sets from their points
             self.graph = self.graphs
             return
         g = torch.cuda.CUDAGraph()
@@ -236,11 +247,21 @@ class FusedStep:
             self._body()
         self.graph = g
 
-    def step(self, x_host=None):
+    def step(self, x_host=None, x_next=None):
         """One training step; returns the device loss.  In host mode x_host
         (n, xd) float32, ideally pinned, is copied in first and the loss is
-        copied back to ``loss_host`` (read it after a synchronisation)."""
-        if self.host:
+        copied back to ``loss_host`` (read it after a synchronisation); when
+        pipelined, x_next holds the next step's points (x_host is then read
+        only on the first call: later steps use the previous call's x_next)."""
+        if self.host and self.pipeline:
+            if x_next is None:
+                raise ValueError("a pipelined host-point step needs the next step's points (x_next)")
+            if not self.started:
+                self.sets[self.cur].x.copy_(x_host, non_blocking=True)
+                self.sets[self.cur].rebuild()
+                self.started = True
+            self.sets[1 - self.cur].x.copy_(x_next, non_blocking=True)
+        elif self.host:
             self.ps.x.copy_(x_host, non_blocking=True)
         if self.pipeline:
             if self.use_graph:

@@ -384,6 +384,36 @@ def test_pipelined_resampling_matches_serial_steps(cuda):
         assert torch.equal(theta, ref[0])
 
 
+def test_pipelined_host_points_match_serial_steps(cuda):
+    """Host-fed points: copying the next step's points in and building their
+    lists on a second stream during the current step gives bit-identical
+    parameters and losses to the serial host-point step (graph and eager)."""
+    from fbpinns_gb300.trainers import FusedStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=3)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    g = torch.Generator().manual_seed(9)
+    batches = [torch.rand((1 << 14, 2), generator=g).pin_memory() for _ in range(6)]
+    results = []
+    for pipeline, use_graph in ((False, True), (True, True), (True, False)):
+        eng = _engine(static, layers, 3 | _lib.D2_LAPLACIAN, chunk=512)
+        st = FusedStep(eng, spec, adam(1e-3), host_points=1 << 14, x_probe=batches[0], use_graph=use_graph,
+                       pipeline=pipeline)
+        losses = []
+        for k in range(5):
+            st.step(batches[k], batches[k + 1])
+            torch.cuda.synchronize()
+            losses.append(float(st.loss_host.item()))
+        st.check()
+        results.append((eng.theta.cpu().clone(), losses))
+    ref = results[0]
+    for theta, losses in results[1:]:
+        assert losses == ref[1]
+        assert torch.equal(theta, ref[0])
+
+
 def test_resampled_steps_match_oracle_points(cuda):
     """The points drawn on the device are uniform in the box and each step's
     interaction lists equal the oracle's for those points."""
