@@ -128,6 +128,10 @@ struct Cfg {
     __host__ __device__ static constexpr int slot_dims(int s) { return d2_slot_dims<D2>(s); }
 };
 
+// Two independent FP32 FMAs a*b + c in one packed instruction (sm_100 and
+// later); each half is rounded exactly like fmaf, so results are unchanged.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // the sorted pair record (point-major pair index, point, slot, 0)
 __device__ __forceinline__ int4 pair_rec(const fbp_pairs& pr, int64_t e) {
     return __ldg(reinterpret_cast<const int4*>(pr.sd_rec) + e);
@@ -139,9 +143,10 @@ struct SParams {
     float b1[C::H1];
     float cw[C::H1 * C::XD];   // W1[n][d] / sd[d]: first-layer tangent along d
     float c2[C::H1 * (C::NS > 0 ? C::NS : 1)];  // per slot s: sum of cw[n][d]^2 over its dims
-    float W2t[C::TWO ? C::H1 * C::H2 : 4];  // [n][k]
-    float W2[C::TWO ? C::H2 * C::H1 : 4];   // [k][n]
-    float b2[C::TWO ? C::H2 : 4];
+    // 16-byte aligned: the layer-2 loops read pairs of neighbouring weights
+    alignas(16) float W2t[C::TWO ? C::H1 * C::H2 : 4];  // [n][k]
+    alignas(16) float W2[C::TWO ? C::H2 * C::H1 : 4];   // [k][n]
+    alignas(16) float b2[C::TWO ? C::H2 : 4];
     float W3[C::HL];
     float b3;
     // activation parameters sigma(z) = c f(o z) of the hidden neurons (adaptive networks)
@@ -387,24 +392,36 @@ __device__ __forceinline__ float l1_act(const SParams<C>& S, const float (&xn)[C
 template <class C>
 __device__ __forceinline__ void l2_chunk(const SParams<C>& S, const float* a1row, int stride, int k0,
                                          float (&acc)[C::KC][C::J]) {
+    // neurons k, k+1 share one packed FMA (fma2: two FP32 FMAs, each rounded like fmaf)
+    static_assert(C::KC % 2 == 0 && C::H2 % 2 == 0, "layer-2 neurons in pairs");
+    constexpr int K2 = C::KC / 2;
+    float2 acc2[K2][C::J];
+    const float2* b2 = reinterpret_cast<const float2*>(&S.b2[k0]);
 #pragma unroll
-    for (int k = 0; k < C::KC; ++k) {
-        acc[k][0] = S.b2[k0 + k];
+    for (int k = 0; k < K2; ++k) {
+        acc2[k][0] = b2[k];
 #pragma unroll
-        for (int c = 1; c < C::J; ++c) acc[k][c] = 0.f;
+        for (int c = 1; c < C::J; ++c) acc2[k][c] = make_float2(0.f, 0.f);
     }
 #pragma unroll 2
     for (int n = 0; n < C::H1; ++n) {
         float v[C::J];
         l1_jet<C>(S, n, a1row[n * stride], v);
-        const float* wrow = &S.W2t[n * C::H2 + k0];
+        const float2* wrow = reinterpret_cast<const float2*>(&S.W2t[n * C::H2 + k0]);
 #pragma unroll
-        for (int k = 0; k < C::KC; ++k) {
-            const float w = wrow[k];
+        for (int k = 0; k < K2; ++k) {
+            const float2 w = wrow[k];
 #pragma unroll
-            for (int c = 0; c < C::J; ++c) acc[k][c] = fmaf(w, v[c], acc[k][c]);
+            for (int c = 0; c < C::J; ++c) acc2[k][c] = fma2(w, make_float2(v[c], v[c]), acc2[k][c]);
         }
     }
+#pragma unroll
+    for (int k = 0; k < K2; ++k)
+#pragma unroll
+        for (int c = 0; c < C::J; ++c) {
+            acc[2 * k][c] = acc2[k][c].x;
+            acc[2 * k + 1][c] = acc2[k][c].y;
+        }
 }
 
 // Network output jet (before unnormalisation) for one pair; a1row/stride is the
@@ -755,10 +772,13 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                 if (act) {
                     float vb[NC][J];
                     if constexpr (C::TWO) {
+                        // first-layer neurons q, q+1 share one packed FMA
+                        static_assert(NC % 2 == 0, "layer-1 neurons in pairs");
+                        float2 vb2[NC / 2][J];
 #pragma unroll
-                        for (int q = 0; q < NC; ++q)
+                        for (int q = 0; q < NC / 2; ++q)
 #pragma unroll
-                            for (int c = 0; c < J; ++c) vb[q][c] = 0.f;
+                            for (int c = 0; c < J; ++c) vb2[q][c] = make_float2(0.f, 0.f);
                         const float* zrow = &R.zb[lane * A::ZS];
 #pragma unroll 1
                         for (int k0 = 0; k0 < H2; k0 += 4) {
@@ -767,18 +787,25 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             for (int c = 0; c < J; ++c) z4[c] = *reinterpret_cast<const float4*>(zrow + c * H2 + k0);
 #pragma unroll
                             for (int kq = 0; kq < 4; ++kq) {
-                                const float* w2 = &S.W2[(k0 + kq) * H1 + n0];
+                                const float2* w2 = reinterpret_cast<const float2*>(&S.W2[(k0 + kq) * H1 + n0]);
 #pragma unroll
-                                for (int q = 0; q < NC; ++q) {
-                                    const float w = w2[q];
+                                for (int q = 0; q < NC / 2; ++q) {
+                                    const float2 w = w2[q];
 #pragma unroll
                                     for (int c = 0; c < J; ++c) {
                                         const float zc = kq == 0 ? z4[c].x : kq == 1 ? z4[c].y : kq == 2 ? z4[c].z : z4[c].w;
-                                        vb[q][c] = fmaf(w, zc, vb[q][c]);
+                                        vb2[q][c] = fma2(w, make_float2(zc, zc), vb2[q][c]);
                                     }
                                 }
                             }
                         }
+#pragma unroll
+                        for (int q = 0; q < NC / 2; ++q)
+#pragma unroll
+                            for (int c = 0; c < J; ++c) {
+                                vb[2 * q][c] = vb2[q][c].x;
+                                vb[2 * q + 1][c] = vb2[q][c].y;
+                            }
                     } else {
 #pragma unroll
                         for (int q = 0; q < NC; ++q) {
@@ -839,13 +866,14 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                     if (b < A::NBLK) {
                         const int nb = b % (H1 / A::NB), kb = b / (H1 / A::NB);
                         const int n0 = nb * A::NB, k0 = kb * A::KB;
-                        float sacc[A::KB][A::NB][J];
+                        // rows k0+2i, k0+2i+1 of the block share one packed FMA
+                        float2 sacc[A::KB / 2][A::NB][J];
 #pragma unroll
-                        for (int i = 0; i < A::KB; ++i)
+                        for (int i = 0; i < A::KB / 2; ++i)
 #pragma unroll
                             for (int q = 0; q < A::NB; ++q)
 #pragma unroll
-                                for (int c = 0; c < J; ++c) sacc[i][q][c] = 0.f;
+                                for (int c = 0; c < J; ++c) sacc[i][q][c] = make_float2(0.f, 0.f);
                         float b2s[A::KB] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 2
                         for (int t = 0; t < nt; ++t) {
@@ -872,11 +900,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                 }
 #pragma unroll
                                 for (int q = 0; q < A::NB; ++q) {
-                                    const float mm = m[q][mi];
-                                    sacc[0][q][c] = fmaf(z4.x, mm, sacc[0][q][c]);
-                                    sacc[1][q][c] = fmaf(z4.y, mm, sacc[1][q][c]);
-                                    sacc[2][q][c] = fmaf(z4.z, mm, sacc[2][q][c]);
-                                    sacc[3][q][c] = fmaf(z4.w, mm, sacc[3][q][c]);
+                                    const float2 mm = make_float2(m[q][mi], m[q][mi]);
+                                    sacc[0][q][c] = fma2(make_float2(z4.x, z4.y), mm, sacc[0][q][c]);
+                                    sacc[1][q][c] = fma2(make_float2(z4.z, z4.w), mm, sacc[1][q][c]);
                                 }
                             }
                         }
@@ -885,12 +911,15 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                             for (int q = 0; q < A::NB; ++q) {
                                 const int n = n0 + q;
-                                float v = sacc[i][q][0];
+                                float s[J];
 #pragma unroll
-                                for (int d = 0; d < XD; ++d) v = fmaf(S.cw[n * XD + d], sacc[i][q][1 + d], v);
+                                for (int c = 0; c < J; ++c) s[c] = (i & 1) ? sacc[i / 2][q][c].y : sacc[i / 2][q][c].x;
+                                float v = s[0];
+#pragma unroll
+                                for (int d = 0; d < XD; ++d) v = fmaf(S.cw[n * XD + d], s[1 + d], v);
 #pragma unroll
                                 for (int ss = 0; ss < C::NS; ++ss)
-                                    v = fmaf(S.c2[n * C::NS + ss], sacc[i][q][1 + XD + ss], v);
+                                    v = fmaf(S.c2[n * C::NS + ss], s[1 + XD + ss], v);
                                 R.gW2[(k0 + i) * H1 + n] += v;
                             }
                         if (nb == 0) {
