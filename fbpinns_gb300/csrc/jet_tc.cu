@@ -11,11 +11,16 @@ static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs
                              int32_t* status, int grid, cudaStream_t st) {
     using C = Cfg<XD, 16, 16, D2>;
     FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward_tc: nparam %d != %d for this shape", net.nparam, C::P);
-    const size_t shm = sizeof(TcSmem<C>);
-    static int res_dev[FBP_MAX_DEVICES] = {};  // per device
+    struct Launch {
+        int res;     // resident CTAs per SM
+        size_t shm;  // dynamic shared memory per CTA
+    };
+    static Launch launch_dev[FBP_MAX_DEVICES] = {};  // per device
     const int dev = current_device();
-    int& res = res_dev[dev];
-    if (!res) {
+    Launch& L = launch_dev[dev];
+    constexpr int cols = TcSmem<C>::COLS;
+    if (!L.res) {
+        size_t shm = sizeof(TcSmem<C>);
         FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)shm));
         // CTAs that fit on one SM by shared memory, registers and threads: an
@@ -28,15 +33,26 @@ static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
         const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the driver's 1 KiB per CTA
         const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
-        res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
+        int res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
         FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");
+        // every resident CTA holds COLS of the SM's 512 TMEM columns; a CTA
+        // beyond that would block in tcgen05.alloc, so the shared-memory
+        // request is padded until no more than 512 / COLS CTAs fit
+        const int max_res = 512 / cols;
+        if (res > max_res) {
+            const int pad_cta = smem_sm / max_res;  // (max_res + 1) * pad_cta > smem_sm
+            shm = (size_t)(pad_cta - (int)fa.sharedSizeBytes - 1024);
+            FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+            res = max_res;
+        }
+        L.shm = shm;
+        L.res = res;
     }
-    // every resident CTA holds COLS of the SM's 512 TMEM columns; more
-    // resident CTAs than that would block in tcgen05.alloc
-    constexpr int cols = TcSmem<C>::COLS;
+    const int res = L.res;
     FBP_REQUIRE(res * cols <= 512, FBP_ERR_UNSUPPORTED, "forward_tc: %d CTAs/SM x %d TMEM columns > 512", res, cols);
     if (grid <= 0) grid = res * sm_count();
-    forward_pairs_tc_kernel<C><<<grid, TC_TILE, shm, st>>>(net, x, pr, pair_out, status);
+    forward_pairs_tc_kernel<C><<<grid, TC_TILE, L.shm, st>>>(net, x, pr, pair_out, status);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
 }

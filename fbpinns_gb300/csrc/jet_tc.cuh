@@ -118,9 +118,12 @@ constexpr uint64_t TC_WAIT_NS = 200000000ull;  // 0.2 s: an MMA group takes micr
 template <class C>
 struct TcSmem {
     static_assert(C::TWO && C::H1 == 16 && C::H2 == 16 && C::J <= 8, "tensor-core shape");
-    // TMEM columns allocated per CTA: J accumulators of 16 columns, rounded up
-    // to the power of two >= 32 that tcgen05.alloc takes
-    static constexpr int COLS = pow2_at_least(C::J * 16 < 32 ? 32 : C::J * 16);
+    // TMEM accumulator buffers: two (the next tile's MMAs run during this
+    // tile's epilogue) when both fit in 128 columns, else one
+    static constexpr int NBUF = 2 * C::J * 16 <= 128 ? 2 : 1;
+    // TMEM columns allocated per CTA: NBUF x J accumulators of 16 columns,
+    // rounded up to the power of two >= 32 that tcgen05.alloc takes
+    static constexpr int COLS = pow2_at_least(NBUF * C::J * 16 < 32 ? 32 : NBUF * C::J * 16);
     static constexpr int NA = C::NS > 0 ? 3 : 2;  // A operands: a, tp (, tpp)
     // A operands, hi and lo, each 128 rows x 16 TF32 = 8 KiB
     float a[NA][2][TC_TILE * 16];
@@ -136,12 +139,54 @@ __host__ __device__ constexpr int tc_a_of(int c) {
     return c == 0 ? 0 : (c <= C::XD ? 1 : 2);
 }
 
+// The rest of the jet for one tile on the CUDA cores: this thread's TMEM lane
+// (its pair) of the layer-2 accumulators at taddr -> tanh rules, output layer,
+// unnormalisation, window product -> the pair's record.
+template <class C>
+__device__ __forceinline__ void tc_epilogue(const SParams<C>& S, uint32_t taddr, int warp, bool act,
+                                            const float (&w)[C::J], int pos, float* __restrict__ pair_out) {
+    constexpr int J = C::J, RS = rec_stride(C::J), H2 = 16;
+    float acc[J][16];
+#pragma unroll
+    for (int c = 0; c < J; ++c) tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), acc[c]);
+    tmem_wait_ld();
+    if (!act) return;
+    float o[J];
+#pragma unroll
+    for (int c = 0; c < J; ++c) o[c] = 0.f;
+    o[0] = S.b3;
+#pragma unroll
+    for (int k = 0; k < H2; ++k) {
+        float z[J], g[J], a, tp, tpp, tppp;
+#pragma unroll
+        for (int c = 0; c < J; ++c) z[c] = acc[c][k];
+        z[0] += S.b2[k];
+        tanh_jet<C>(z, g, a, tp, tpp, tppp);
+        const float w3 = S.W3[k];
+#pragma unroll
+        for (int c = 0; c < J; ++c) o[c] = fmaf(w3, g[c], o[c]);
+    }
+    float u[J];
+#pragma unroll
+    for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
+    u[0] += S.mu_u;
+    float rec[RS];
+    product_jet<C>(u, w, rec);
+#pragma unroll
+    for (int c = 0; c < J; ++c) rec[J + c] = w[c];
+#pragma unroll
+    for (int c = 2 * J; c < RS; ++c) rec[c] = 0.f;
+    float4* dst = reinterpret_cast<float4*>(pair_out + (size_t)pos * RS);
+#pragma unroll
+    for (int q = 0; q < RS / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
+}
+
 template <class C>
 __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, const float* __restrict__ x,
                                                                     fbp_pairs pr, float* __restrict__ pair_out,
                                                                     int32_t* __restrict__ status) {
     constexpr int J = C::J, XD = C::XD, RS = rec_stride(C::J), H1 = 16, H2 = 16;
-    constexpr int NA = TcSmem<C>::NA;
+    constexpr int NA = TcSmem<C>::NA, NBUF = TcSmem<C>::NBUF;
     __shared__ SParams<C> S;
     extern __shared__ float4 dyn_smem[];
     TcSmem<C>& T = *reinterpret_cast<TcSmem<C>*>(dyn_smem);
@@ -195,68 +240,87 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
 #pragma unroll
             for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
         }
-        for (int t0 = 0; t0 < cnt; t0 += TC_TILE) {
-            const bool act = t0 + tid < cnt;
+        // Software pipeline over the item's tiles: iteration ti stages tile ti
+        // and issues its MMAs into TMEM buffer ti % NBUF, then runs the epilogue
+        // of tile ti-1 (from the other buffer) while those MMAs execute, then
+        // waits for them.  A rows are rewritten only after that wait; a TMEM
+        // buffer is rewritten only by MMAs issued after the staging barrier
+        // that follows every thread's read of it.
+        const int ntile = (cnt + TC_TILE - 1) / TC_TILE;
+        int pos_p = 0;        // tile ti-1: this thread's pair record index,
+        bool act_p = false;   // whether it has a pair,
+        float w_p[J];         // and its window jet
+#pragma unroll
+        for (int c = 0; c < J; ++c) w_p[c] = 0.f;
+        for (int ti = 0; ti <= ntile; ++ti) {
+            const int t0 = ti * TC_TILE;
+            const bool stage = ti < ntile;
+            const bool act = stage && t0 + tid < cnt;
             const int pos = pos_n;
             float xn[XD];
 #pragma unroll
             for (int d = 0; d < XD; ++d) xn[d] = (xr_n[d] - S.mu[d]) * S.inv_sd[d];
-            // this pair's rows of the A operands
+            if (stage) {
+                // this pair's rows of the A operands
 #pragma unroll
-            for (int n4 = 0; n4 < H1; n4 += 4) {
-                float av[NA][4];
+                for (int n4 = 0; n4 < H1; n4 += 4) {
+                    float av[NA][4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    float a, tp, tpp, tppp;
-                    C::AF::derivs(l1_act<C>(S, xn, n4 + q), 1.0f, 1.0f, a, tp, tpp, tppp);
-                    av[0][q] = a;
-                    av[1][q] = tp;
-                    if constexpr (NA > 2) av[NA - 1][q] = tpp;
-                }
-                const uint32_t off = kmajor16_off(tid, n4) >> 2;
+                    for (int q = 0; q < 4; ++q) {
+                        float a, tp, tpp, tppp;
+                        C::AF::derivs(l1_act<C>(S, xn, n4 + q), 1.0f, 1.0f, a, tp, tpp, tppp);
+                        av[0][q] = a;
+                        av[1][q] = tp;
+                        if constexpr (NA > 2) av[NA - 1][q] = tpp;
+                    }
+                    const uint32_t off = kmajor16_off(tid, n4) >> 2;
 #pragma unroll
-                for (int o = 0; o < NA; ++o) {
-                    float h[4], l[4];
+                    for (int o = 0; o < NA; ++o) {
+                        float h[4], l[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) split_tf32(av[o][q], h[q], l[q]);
-                    *reinterpret_cast<float4*>(&T.a[o][0][off]) = make_float4(h[0], h[1], h[2], h[3]);
-                    *reinterpret_cast<float4*>(&T.a[o][1][off]) = make_float4(l[0], l[1], l[2], l[3]);
-                }
-            }
-            fence_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0) {
-#pragma unroll
-                for (int c = 0; c < J; ++c) {
-                    const int o = tc_a_of<C>(c);
-                    const uint32_t ah = smem_u32(&T.a[o][0][0]), al = smem_u32(&T.a[o][1][0]);
-                    const uint32_t bh = smem_u32(&T.b[c][0][0]), bl = smem_u32(&T.b[c][1][0]);
-                    const uint32_t d = tmem + (uint32_t)(c * 16);
-#pragma unroll
-                    for (int ks = 0; ks < 2; ++ks) {
-                        const uint32_t ko = ks * 256;  // two 16-byte K chunks per MMA (K = 8)
-                        umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, ks > 0);
-                        umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bl + ko, 128, 512), idesc, 1);
-                        umma_tf32(d, umma_desc(al + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, 1);
+                        for (int q = 0; q < 4; ++q) split_tf32(av[o][q], h[q], l[q]);
+                        *reinterpret_cast<float4*>(&T.a[o][0][off]) = make_float4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<float4*>(&T.a[o][1][off]) = make_float4(l[0], l[1], l[2], l[3]);
                     }
                 }
-                umma_commit(mbar);
-            }
-            // prefetch the next tile's pair while the MMAs run
-            const int tn = t0 + TC_TILE + tid;
-            if (tn < cnt) {
-                const int4 r = pair_rec(pr, beg + tn);
-                const int pt = r.y;
-                pos_n = r.x;
+                fence_async_smem();
+                tc_fence_before();
+                __syncthreads();
+                tc_fence_after();
+                if (tid == 0) {
+                    const uint32_t buf = tmem + (uint32_t)((ti % NBUF) * J * 16);
 #pragma unroll
-                for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+                    for (int c = 0; c < J; ++c) {
+                        const int o = tc_a_of<C>(c);
+                        const uint32_t ah = smem_u32(&T.a[o][0][0]), al = smem_u32(&T.a[o][1][0]);
+                        const uint32_t bh = smem_u32(&T.b[c][0][0]), bl = smem_u32(&T.b[c][1][0]);
+                        const uint32_t d = buf + (uint32_t)(c * 16);
+#pragma unroll
+                        for (int ks = 0; ks < 2; ++ks) {
+                            const uint32_t ko = ks * 256;  // two 16-byte K chunks per MMA (K = 8)
+                            umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, ks > 0);
+                            umma_tf32(d, umma_desc(ah + ko, 128, 512), umma_desc(bl + ko, 128, 512), idesc, 1);
+                            umma_tf32(d, umma_desc(al + ko, 128, 512), umma_desc(bh + ko, 128, 512), idesc, 1);
+                        }
+                    }
+                    umma_commit(mbar);
+                }
+                // prefetch the next tile's pair while the MMAs run
+                const int tn = t0 + TC_TILE + tid;
+                if (tn < cnt) {
+                    const int4 r = pair_rec(pr, beg + tn);
+                    const int pt = r.y;
+                    pos_n = r.x;
+#pragma unroll
+                    for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
+                }
             }
-            float w[J];
-            window_jet<C>(S, xn, w);
+            __syncwarp();  // the epilogue's tcgen05.ld is warp-collective
+            if (ti > 0 && NBUF == 2)
+                tc_epilogue<C>(S, tmem + (uint32_t)(((ti - 1) % NBUF) * J * 16), warp, act_p, w_p, pos_p, pair_out);
+            if (!stage) break;
             // every thread waits; the verdict is made CTA-uniform before the
-            // warp-collective tcgen05.ld below
+            // warp-collective tcgen05.ld of the epilogue
             failed = __syncthreads_or(!mbar_wait_bounded(mbar, phase, TC_WAIT_NS));
             if (failed) {
                 if (tid == 0) atomicOr(status, FBP_STATUS_TC_TIMEOUT);
@@ -264,45 +328,17 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             }
             phase ^= 1u;
             tc_fence_after();
-            float acc[J][16];
-#pragma unroll
-            for (int c = 0; c < J; ++c) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), acc[c]);
-            tmem_wait_ld();
-            if (act) {
-                float o[J];
-#pragma unroll
-                for (int c = 0; c < J; ++c) o[c] = 0.f;
-                o[0] = S.b3;
-#pragma unroll
-                for (int k = 0; k < H2; ++k) {
-                    float z[J], g[J], a, tp, tpp;
-#pragma unroll
-                    for (int c = 0; c < J; ++c) z[c] = acc[c][k];
-                    z[0] += S.b2[k];
-                    float tppp;
-                    tanh_jet<C>(z, g, a, tp, tpp, tppp);
-                    const float w3 = S.W3[k];
-#pragma unroll
-                    for (int c = 0; c < J; ++c) o[c] = fmaf(w3, g[c], o[c]);
-                }
-                float u[J];
-#pragma unroll
-                for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
-                u[0] += S.mu_u;
-                float rec[RS];
-                product_jet<C>(u, w, rec);
-#pragma unroll
-                for (int c = 0; c < J; ++c) rec[J + c] = w[c];
-#pragma unroll
-                for (int c = 2 * J; c < RS; ++c) rec[c] = 0.f;
-                float4* dst = reinterpret_cast<float4*>(pair_out + (size_t)pos * RS);
-#pragma unroll
-                for (int q = 0; q < RS / 4; ++q)
-                    dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
+            window_jet<C>(S, xn, w_p);
+            pos_p = pos;
+            act_p = act;
+            if constexpr (NBUF == 1) {
+                // one TMEM buffer: the epilogue runs before the next tile's MMAs
+                __syncwarp();
+                tc_epilogue<C>(S, tmem, warp, act_p, w_p, pos_p, pair_out);
+                tc_fence_before();
+                __syncthreads();
+                tc_fence_after();
             }
-            tc_fence_before();
-            __syncthreads();  // TMEM and the A rows are reused by the next tile
-            tc_fence_after();
         }
     }
     if (failed) mbar_wait_bounded(mbar, phase, TC_WAIT_NS);  // let the timed-out MMAs finish
