@@ -239,7 +239,8 @@ def run_fused(args, world, rank, local):
     tc = False if args.fma_forward else None
     # the Poisson residual needs only the Laplacian: jets (u, u_x, u_y, u_xx + u_yy)
     d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
-    eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
+    eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
+                       dynamic_items=not args.static_items)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
@@ -275,7 +276,8 @@ def run_fused(args, world, rank, local):
     # ---- end to end through the public step API with host buffers ----------
     e2e = None
     try:
-        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc)
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
+                            dynamic_items=not args.static_items)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -428,6 +430,8 @@ def main():
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
+    ap.add_argument("--static-items", action="store_true",
+                    help="jet kernels take work items in a fixed stride instead of from a device counter")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-timed", action="store_true",

@@ -132,6 +132,25 @@ struct Cfg {
 // later); each half is rounded exactly like fmaf, so results are unchanged.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+// Work-item schedule of the persistent jet kernels: with pr.item_ctr null CTA b
+// takes items b, b + gridDim.x, ...; otherwise each CTA takes the next index
+// of the counter (zeroed by the launcher), so a CTA that starts late takes
+// fewer items.  All threads of the CTA call these (they contain barriers; the
+// index is broadcast through *s_item).
+__device__ __forceinline__ int first_item(const fbp_pairs& pr, int* s_item) {
+    if (!pr.item_ctr) return blockIdx.x;
+    if (threadIdx.x == 0) *s_item = atomicAdd(pr.item_ctr, 1);
+    __syncthreads();
+    return *s_item;
+}
+__device__ __forceinline__ int next_item(const fbp_pairs& pr, int it, int* s_item) {
+    if (!pr.item_ctr) return it + gridDim.x;
+    __syncthreads();  // every thread has read the previous index
+    if (threadIdx.x == 0) *s_item = atomicAdd(pr.item_ctr, 1);
+    __syncthreads();
+    return *s_item;
+}
+
 // the sorted pair record (point-major pair index, point, slot, 0)
 __device__ __forceinline__ int4 pair_rec(const fbp_pairs& pr, int64_t e) {
     return __ldg(reinterpret_cast<const int4*>(pr.sd_rec) + e);
@@ -469,8 +488,9 @@ __global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net n
     constexpr int J = C::J, XD = C::XD, RS = rec_stride(C::J);
     __shared__ SParams<C> S;
     __shared__ float a1s[C::H1 * FWD_THREADS];
+    __shared__ int s_item;
     const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
-    for (int it = blockIdx.x; it < nit; it += gridDim.x) {
+    for (int it = first_item(pr, &s_item); it < nit; it = next_item(pr, it, &s_item)) {
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
         load_params<C>(S, net, j);
@@ -608,8 +628,9 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
     extern __shared__ float4 dyn_smem[];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     WarpRows<C>& R = reinterpret_cast<WarpRows<C>*>(dyn_smem)[wid];
+    __shared__ int s_item;
     const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
-    for (int it = blockIdx.x; it < nit; it += gridDim.x) {
+    for (int it = first_item(pr, &s_item); it < nit; it = next_item(pr, it, &s_item)) {
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
         load_params<C>(S, net, j);

@@ -26,6 +26,7 @@ int launch_forward(const fbp_net& net, const float* x, const fbp_pairs& pr, floa
         if (!auto_grid[dev]) auto_grid[dev] = resident_grid(forward_pairs_kernel<C>, FWD_THREADS, 0);
         grid = auto_grid[dev];
     }
+    if (pr.item_ctr) FBP_CUDA_CHECK(cudaMemsetAsync(pr.item_ctr, 0, sizeof(int32_t), st));
     forward_pairs_kernel<C><<<grid, FWD_THREADS, 0, st>>>(net, x, pr, pair_out);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
@@ -48,6 +49,7 @@ int launch_adjoint(const fbp_net& net, const float* x, const fbp_pairs& pr, cons
         if (!auto_grid[dev]) auto_grid[dev] = resident_grid(adjoint_pairs_kernel<C>, AdjW<C>::T, shm);
         grid = auto_grid[dev];
     }
+    if (pr.item_ctr) FBP_CUDA_CHECK(cudaMemsetAsync(pr.item_ctr, 0, sizeof(int32_t), st));
     adjoint_pairs_kernel<C><<<grid, AdjW<C>::T, shm, st>>>(net, x, pr, slot_out, grad_part);
     FBP_LAUNCH_CHECK();
     return FBP_OK;

@@ -52,6 +52,7 @@ static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs
     const int res = L.res;
     FBP_REQUIRE(res * cols <= 512, FBP_ERR_UNSUPPORTED, "forward_tc: %d CTAs/SM x %d TMEM columns > 512", res, cols);
     if (grid <= 0) grid = res * sm_count();
+    if (pr.item_ctr) FBP_CUDA_CHECK(cudaMemsetAsync(pr.item_ctr, 0, sizeof(int32_t), st));
     forward_pairs_tc_kernel<C><<<grid, TC_TILE, L.shm, st>>>(net, x, pr, pair_out, status);
     FBP_LAUNCH_CHECK();
     return FBP_OK;

@@ -209,8 +209,9 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
     constexpr uint32_t idesc = umma_idesc_tf32(TC_TILE, H2);
     uint32_t phase = 0;
     bool failed = false;
+    __shared__ int s_item;
     const int nit = (int)min((int64_t)*pr.n_items, pr.items_cap);
-    for (int it = blockIdx.x; it < nit && !failed; it += gridDim.x) {
+    for (int it = first_item(pr, &s_item); it < nit && !failed; it = next_item(pr, it, &s_item)) {
         const int j = pr.items[3 * (size_t)it], beg = pr.items[3 * (size_t)it + 1], cnt = pr.items[3 * (size_t)it + 2];
         __syncthreads();
         load_params<C, false>(S, net, j);

@@ -139,6 +139,8 @@ class PointSet:
         self.item_start_act = torch.zeros(m + 1, **i32)
         self.n_items_all = torch.zeros(1, **i32)
         self.n_items_act = torch.zeros(1, **i32)
+        # work-item counters of the forward [0] and adjoint [1] launches (dynamic schedule)
+        self.item_ctr = torch.zeros(2, **i32)
         R = record_stride(self.J)
         self.pair_out = torch.empty((max(s_cap, 1), R), dtype=torch.float32, device=dev)
         self.slot_out = torch.empty((max(u_cap, 1), R), dtype=torch.float32, device=dev)
@@ -190,6 +192,8 @@ class PointSet:
             p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
         p.items_cap = self.items_cap
         p.slots_cap = self.slot_out.shape[0]
+        if self.eng.dynamic_items:
+            p.item_ctr = _lib.ptr(self.item_ctr[1 if adjoint else 0])
         return p
 
     def subdomain_counts(self):
@@ -214,7 +218,7 @@ class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None, tensor_cores=None,
-                 activation="tanh"):
+                 activation="tanh", dynamic_items=True):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -248,6 +252,9 @@ class FBPINNEngine:
         self.J = jet_size(self.xd, self.d2mask)
         self.chunk = int(chunk)
         self.launch_grid = int(grid) if grid else 0
+        # the jet kernels' CTAs take work items from a device counter (True) or
+        # in a fixed stride (False); results are the same either way
+        self.dynamic_items = bool(dynamic_items)
         # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
         # None = wherever available, True = required, False = CUDA-core FMA kernel
         tc_ok = tc_supported(self.xd, self.h1, self.h2) and self.act == _lib.ACT_TANH

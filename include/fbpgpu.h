@@ -134,6 +134,12 @@ typedef struct fbp_pairs {
     const int32_t* n_items;   /* device count of valid items */
     int64_t items_cap;
     int64_t slots_cap;        /* rows of the slot buffer; larger slot ids are skipped */
+    /* Optional (NULL: static schedule, CTA b takes items b, b + grid, ...): one
+     * device int32 that the jet launchers zero before each launch and their
+     * CTAs then take items from in turn, so that CTAs delayed by kernels of
+     * other streams take fewer.  The results do not depend on the schedule.
+     * Concurrent launches need distinct counters. */
+    int32_t* item_ctr;
 } fbp_pairs;
 
 /* Built-in PDE residuals fused into the POU/loss kernel. */
