@@ -240,7 +240,7 @@ def run_fused(args, world, rank, local):
     # the Poisson residual needs only the Laplacian: jets (u, u_x, u_y, u_xx + u_yy)
     d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
     eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                       dynamic_items=not args.static_items)
+                       dynamic_items=not args.static_items, forward_chunk=args.forward_chunk)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
@@ -277,7 +277,7 @@ def run_fused(args, world, rank, local):
     e2e = None
     try:
         eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                            dynamic_items=not args.static_items)
+                            dynamic_items=not args.static_items, forward_chunk=args.forward_chunk)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -408,7 +408,7 @@ def run_fused(args, world, rank, local):
                 "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
-                           "parallelism": f"replicas x{world}", "chunk": args.chunk,
+                           "parallelism": f"replicas x{world}", "chunk": args.chunk, "forward_chunk": eng.forward_chunk,
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
@@ -425,7 +425,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
-    ap.add_argument("--chunk", type=int, default=512)
+    ap.add_argument("--chunk", type=int, default=1024, help="pairs per adjoint work item")
+    ap.add_argument("--forward-chunk", type=int, default=0, help="pairs per forward work item (0: 4 x --chunk)")
     ap.add_argument("--grid", type=int, default=0)
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--per-dim-jets", action="store_true",

@@ -101,7 +101,8 @@ class Constants(ConstantsBase):
         self.engine = "fused"          # "fused" (CUDA adjoint + fused loss) or "plain" (torch autograd)
         self.resample = False          # redraw uniform collocation points every step on the device
         self.device = "cuda"
-        self.chunk = 512               # pairs per work item
+        self.chunk = 1024              # pairs per adjoint work item
+        self.forward_chunk = None      # pairs per forward work item (None: 4 x chunk)
         self.launch_grid = 0           # CTAs of the persistent jet kernels (0 = 4 per SM)
         self.use_graph = True          # capture the step in a CUDA graph
         self.tensor_cores = None       # forward jets on tcgen05 (3xTF32): None = where compiled, True, False

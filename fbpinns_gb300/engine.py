@@ -110,7 +110,8 @@ class PointSet:
         self.n = int(x.shape[0])
         self.x = x.to(g.device, torch.float32).contiguous()
         self.J = engine.J
-        self.chunk = int(chunk or engine.chunk)
+        self.chunk = int(chunk or engine.chunk)  # pairs per adjoint work item
+        self.fwd_chunk = max(self.chunk, engine.forward_chunk)  # pairs per forward work item
         self.select = select
         s_cap, u_cap = (None, None) if caps is None else caps
         self.takes = PointTakes(g, self.n, s_cap=s_cap, u_cap=u_cap)
@@ -172,7 +173,7 @@ class PointSet:
         lib = _lib.load()
         st = _lib.stream_ptr(stream)
         ws = self.work_scratch.numel() * 4
-        _lib.check(lib.fbp_build_work(_lib.ptr(self.sd_start), eng.m, None, self.chunk, _lib.ptr(self.items_all),
+        _lib.check(lib.fbp_build_work(_lib.ptr(self.sd_start), eng.m, None, self.fwd_chunk, _lib.ptr(self.items_all),
                                       _lib.ptr(self.item_start_all), _lib.ptr(self.n_items_all), self.items_cap,
                                       _lib.ptr(t_status(self)), _lib.ptr(self.work_scratch), ws, st),
                    "fbp_build_work")
@@ -217,8 +218,8 @@ def tc_supported(xd, h1, h2):
 class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
-    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=512, grid=None, tensor_cores=None,
-                 activation="tanh", dynamic_items=True):
+    def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
+                 activation="tanh", dynamic_items=True, forward_chunk=None):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -251,6 +252,9 @@ class FBPINNEngine:
                 f"add the shape to csrc/jet_inst_*.cu")
         self.J = jet_size(self.xd, self.d2mask)
         self.chunk = int(chunk)
+        # forward work items may be longer: its per-item set-up (weights, B
+        # operands, the tile pipeline's fill and drain) is larger
+        self.forward_chunk = int(forward_chunk) if forward_chunk else 4 * self.chunk
         self.launch_grid = int(grid) if grid else 0
         # the jet kernels' CTAs take work items from a device counter (True) or
         # in a fixed stride (False); results are the same either way

@@ -363,7 +363,8 @@ class FBPINNTrainer:
                                          _lib.ACTIVATIONS[activation]):
                 d2 = d2g
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
-                           tensor_cores=getattr(c, "tensor_cores", None), activation=activation)
+                           tensor_cores=getattr(c, "tensor_cores", None), activation=activation,
+                           forward_chunk=getattr(c, "forward_chunk", None))
         eng.set_theta(pack_layers(net_tr["layers"]))
         for k, v in list(all_params["trainable"].get("problem", {}).items()):
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()

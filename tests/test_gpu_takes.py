@@ -140,14 +140,17 @@ def test_sort_and_work_queue(cuda):
     np.testing.assert_array_equal(_np(ps.sd_slot[:s]), _np(ps.takes.p_take[:s])[order])
     counts = np.bincount(m_take, minlength=static["m"])
     np.testing.assert_array_equal(_np(ps.sd_start), np.concatenate([[0], np.cumsum(counts)]))
-    nit = int(ps.n_items_all.item())
-    items = _np(ps.items_all[: 3 * nit]).reshape(-1, 3)
-    cover = np.zeros(s, dtype=np.int64)
-    for j, b, c in items:
-        assert 0 < c <= 256
-        assert m_take[order[b:b + c]].tolist() == [j] * c
-        cover[b:b + c] += 1
-    assert (cover == 1).all()
+    # forward items of up to 4 x 256 pairs (the engine's default), adjoint items of up to 256
+    assert ps.fwd_chunk == 1024 and ps.chunk == 256
+    for n_items, queue, chunk in ((ps.n_items_all, ps.items_all, 1024), (ps.n_items_act, ps.items_act, 256)):
+        nit = int(n_items.item())
+        items = _np(queue[: 3 * nit]).reshape(-1, 3)
+        cover = np.zeros(s, dtype=np.int64)
+        for j, b, c in items:
+            assert 0 < c <= chunk
+            assert m_take[order[b:b + c]].tolist() == [j] * c
+            cover[b:b + c] += 1
+        assert (cover == 1).all()
 
 
 @pytest.mark.slow
