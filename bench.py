@@ -240,7 +240,7 @@ def run_fused(args, world, rank, local):
     # the Poisson residual needs only the Laplacian: jets (u, u_x, u_y, u_xx + u_yy)
     d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
     eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                       dynamic_items=not args.static_items, forward_chunk=args.forward_chunk)
+                       schedule=args.schedule, forward_chunk=args.forward_chunk)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
@@ -277,7 +277,7 @@ def run_fused(args, world, rank, local):
     e2e = None
     try:
         eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                            dynamic_items=not args.static_items, forward_chunk=args.forward_chunk)
+                            schedule=args.schedule, forward_chunk=args.forward_chunk)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -408,7 +408,7 @@ def run_fused(args, world, rank, local):
                 "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
-                           "parallelism": f"replicas x{world}", "chunk": args.chunk, "forward_chunk": eng.forward_chunk,
+                           "parallelism": f"replicas x{world}", "chunk": args.chunk, "forward_chunk": eng.forward_chunk, "schedule": eng.schedule,
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
@@ -431,8 +431,8 @@ def main():
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
-    ap.add_argument("--static-items", action="store_true",
-                    help="jet kernels take work items in a fixed stride instead of from a device counter")
+    ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "per_item"],
+                    help="how the jet kernels' CTAs take work items")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-timed", action="store_true",

@@ -99,6 +99,9 @@ _SIG = {
                            _P, _P]),
     "fbp_sample_uniform": (C.c_int, [_P, _I64, _I32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64,
                                      C.c_uint64, _P, _P]),
+    "fbp_graph_instantiate": (C.c_int, [_P, _I32, C.POINTER(C.c_void_p)]),
+    "fbp_graph_launch": (C.c_int, [_P, _P]),
+    "fbp_graph_exec_destroy": (C.c_int, [_P]),
     "fbp_fma_probe": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_double), _P]),
     "fbp_tanh_probe": (C.c_int, [_P, _P, _I64, _P]),
     "fbp_has_shape": (C.c_int, [_I32, _I32, _I32, _I32, _I32]),

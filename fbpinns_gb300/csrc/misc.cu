@@ -179,6 +179,26 @@ extern "C" int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double*
     return FBP_OK;
 }
 
+extern "C" int fbp_graph_instantiate(void* graph, int32_t use_node_priority, void** exec_out) {
+    FBP_REQUIRE(graph && exec_out, FBP_ERR_INVALID, "fbp_graph_instantiate: null argument");
+    cudaGraphExec_t ex = nullptr;
+    const unsigned long long flags = use_node_priority ? cudaGraphInstantiateFlagUseNodePriority : 0;
+    FBP_CUDA_CHECK(cudaGraphInstantiateWithFlags(&ex, static_cast<cudaGraph_t>(graph), flags));
+    *exec_out = ex;
+    return FBP_OK;
+}
+
+extern "C" int fbp_graph_launch(void* exec, void* stream) {
+    FBP_REQUIRE(exec, FBP_ERR_INVALID, "fbp_graph_launch: null graph");
+    FBP_CUDA_CHECK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(exec), as_stream(stream)));
+    return FBP_OK;
+}
+
+extern "C" int fbp_graph_exec_destroy(void* exec) {
+    if (exec) FBP_CUDA_CHECK(cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec)));
+    return FBP_OK;
+}
+
 extern "C" int fbp_fma_probe(float* sink, int32_t blocks, int32_t iters, double* flops_out, void* stream) {
     FBP_REQUIRE(sink && flops_out && blocks > 0 && iters > 0, FBP_ERR_INVALID, "fbp_fma_probe: bad args");
     fma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(sink, iters);

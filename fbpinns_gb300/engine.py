@@ -134,6 +134,7 @@ class PointSet:
         self.sort_scratch = torch.empty(int(lib.fbp_sort_scratch_bytes(s_cap, m)) // 4 + 1, **i32)
         self.work_scratch = torch.empty(int(lib.fbp_work_scratch_bytes(m)) // 4 + 1, **i32)
         self.items_cap = s_cap // self.chunk + m + 1
+        self.forward_items_cap = s_cap // self.fwd_chunk + m + 1  # the forward queue's items fit in this
         self.items_all = torch.zeros(3 * self.items_cap, **i32)
         self.items_act = torch.zeros(3 * self.items_cap, **i32)
         self.item_start_all = torch.zeros(m + 1, **i32)
@@ -193,7 +194,7 @@ class PointSet:
             p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
         p.items_cap = self.items_cap
         p.slots_cap = self.slot_out.shape[0]
-        if self.eng.dynamic_items:
+        if self.eng.schedule == "dynamic":
             p.item_ctr = _lib.ptr(self.item_ctr[1 if adjoint else 0])
         return p
 
@@ -219,7 +220,7 @@ class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
-                 activation="tanh", dynamic_items=True, forward_chunk=None):
+                 activation="tanh", schedule="dynamic", forward_chunk=None):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -256,9 +257,15 @@ class FBPINNEngine:
         # operands, the tile pipeline's fill and drain) is larger
         self.forward_chunk = int(forward_chunk) if forward_chunk else 4 * self.chunk
         self.launch_grid = int(grid) if grid else 0
-        # the jet kernels' CTAs take work items from a device counter (True) or
-        # in a fixed stride (False); results are the same either way
-        self.dynamic_items = bool(dynamic_items)
+        # how the jet kernels' CTAs take work items (the results do not depend on it):
+        #   "dynamic"   a resident grid; each CTA takes the next item from a device counter
+        #   "static"    a resident grid; CTA b takes items b, b + grid, ...
+        #   "per_item"  one CTA per item (grid = the queue's capacity); CTAs retire
+        #               as they finish, so kernels of a higher-priority stream get
+        #               SM slots during the launch
+        if schedule not in ("dynamic", "static", "per_item"):
+            raise ValueError(f"schedule must be 'dynamic', 'static' or 'per_item', not {schedule!r}")
+        self.schedule = schedule
         # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
         # None = wherever available, True = required, False = CUDA-core FMA kernel
         tc_ok = tc_supported(self.xd, self.h1, self.h2) and self.act == _lib.ACT_TANH
@@ -326,13 +333,14 @@ class FBPINNEngine:
         lib = _lib.load()
         net = self.net_struct(theta)
         pr = ps.pairs_struct(False)
+        grid = ps.forward_items_cap if self.schedule == "per_item" else self.launch_grid
         if self.tensor_cores:
             _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
-                                                _lib.ptr(ps.takes.status), 0, _lib.stream_ptr(stream)),
+                                                _lib.ptr(ps.takes.status), grid, _lib.stream_ptr(stream)),
                        "fbp_forward_pairs_tc")
             return
         _lib.check(lib.fbp_forward_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
-                                         self.launch_grid, _lib.stream_ptr(stream)), "fbp_forward_pairs")
+                                         grid, _lib.stream_ptr(stream)), "fbp_forward_pairs")
 
     def pou_forward(self, ps, stream=None):
         lib = _lib.load()
@@ -371,8 +379,9 @@ class FBPINNEngine:
         st = _lib.stream_ptr(stream)
         net = self.net_struct(theta)
         pr = ps.pairs_struct(True)
+        grid = ps.items_cap if self.schedule == "per_item" else self.launch_grid
         _lib.check(lib.fbp_adjoint_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
-                                         _lib.ptr(ps.grad_part), self.launch_grid, st), "fbp_adjoint_pairs")
+                                         _lib.ptr(ps.grad_part), grid, st), "fbp_adjoint_pairs")
         if not reduce:
             return None
         return self.reduce_grad(ps, out, stream)

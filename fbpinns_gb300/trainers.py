@@ -13,6 +13,7 @@ report (summary line, test L1, model pickles).  The step itself is one of:
   gradient comes back through the CUDA adjoint.
 """
 
+import ctypes
 import logging
 import os
 import pickle
@@ -105,6 +106,34 @@ class GenericStep:
                                 opt["eps_root"])
         eng.adam(opt["learning_rate"], opt["b1"], opt["b2"], opt["eps"], opt["eps_root"], grad=gtheta)
         return loss
+
+
+class StepGraph:
+    """A captured CUDA graph instantiated by the library with per-node
+    priorities: kernel nodes keep the priority of the stream they were captured
+    on (torch's own replay would run every node at the launching stream's
+    priority).  Owns torch's graph (and its memory pool) and the executable."""
+
+    def __init__(self):
+        self.graph = torch.cuda.CUDAGraph(keep_graph=True)
+        self.exec = None
+
+    def instantiate(self):
+        lib = _lib.load()
+        out = ctypes.c_void_p()
+        _lib.check(lib.fbp_graph_instantiate(ctypes.c_void_p(self.graph.raw_cuda_graph()), 1, ctypes.byref(out)),
+                   "fbp_graph_instantiate")
+        self.exec = out
+
+    def replay(self):
+        _lib.check(_lib.load().fbp_graph_launch(self.exec, _lib.stream_ptr()), "fbp_graph_launch")
+
+    def __del__(self):
+        if self.exec is not None and _lib is not None:
+            try:
+                _lib.load().fbp_graph_exec_destroy(self.exec)
+            except Exception:  # interpreter shutdown
+                pass
 
 
 class FusedStep:
@@ -231,9 +260,10 @@ class FusedStep:
             dst.copy_(src)
         if self.pipeline:
             for cur in (0, 1):
-                g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g):
+                g = StepGraph()
+                with torch.cuda.graph(g.graph):
                     self._body_pipelined(cur)
+                g.instantiate()
                 self.graphs[cur] = g
             if self.resample is not None:
                 self.cur = 0

@@ -340,6 +340,17 @@ int fbp_adam(float* theta, float* m1, float* m2, const float* grad, const uint8_
 int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, const double* xmax,
                        uint64_t seed, uint64_t offset, const int32_t* counter, void* stream);
 
+/* Executable graph of a captured training step (cudaGraph_t graph) whose
+ * kernel nodes keep the priority of the stream they were captured from
+ * (graph instantiated with cudaGraphInstantiateFlagUseNodePriority), so
+ * that the next step's interaction lists, captured on a high-priority
+ * stream, take SM slots ahead of the step's own kernels.  Replaces the
+ * reference's jit/AOT compile of the update (fbpinns/trainers.py:650-652);
+ * *exec_out is released by fbp_graph_exec_destroy. */
+int fbp_graph_instantiate(void* graph, int32_t use_node_priority, void** exec_out);
+int fbp_graph_launch(void* exec, void* stream);
+int fbp_graph_exec_destroy(void* exec);
+
 /* FP32 FMA throughput probe used for the roofline denominator: runs
  * `iters` dependent-chain FMA loops on every SM; *flops_out (host) gets the
  * flop count of the launch. */

@@ -384,6 +384,34 @@ def test_pipelined_resampling_matches_serial_steps(cuda):
         assert torch.equal(theta, ref[0])
 
 
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_work_item_schedules_give_identical_steps(cuda, tensor_cores):
+    """The dynamic (device counter), static-stride and one-CTA-per-item
+    schedules of the jet kernels give bitwise the same loss and parameters,
+    and so do different resident grids."""
+    from fbpinns_gb300.optim import adam
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=4)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    x = torch.rand((1 << 14, 2), generator=torch.Generator().manual_seed(3))
+    results = []
+    for schedule, grid in (("dynamic", None), ("static", None), ("per_item", None), ("dynamic", 37), ("static", 37)):
+        eng = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=256, grid=grid,
+                           schedule=schedule, tensor_cores=tensor_cores)
+        eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
+        eng.set_problem(spec)
+        ps = eng.points(x)
+        opt = adam(1e-3)
+        losses = [eng.fused_step(ps, opt["learning_rate"]).item() for _ in range(3)]
+        torch.cuda.synchronize()
+        ps.check_status()
+        results.append((losses, eng.theta.cpu().clone()))
+    for losses, theta in results[1:]:
+        assert losses == results[0][0]
+        assert torch.equal(theta, results[0][1])
+
+
 def test_pipelined_host_points_match_serial_steps(cuda):
     """Host-fed points: copying the next step's points in and building their
     lists on a second stream during the current step gives bit-identical
