@@ -131,6 +131,9 @@ struct Cfg {
 // Two independent FP32 FMAs a*b + c in one packed instruction (sm_100 and
 // later); each half is rounded exactly like fmaf, so results are unchanged.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 
 // Work-item schedule of the persistent jet kernels: with pr.item_ctr null CTA b
 // takes items b, b + gridDim.x, ...; otherwise each CTA takes the next index
@@ -159,14 +162,14 @@ __device__ __forceinline__ int4 pair_rec(const fbp_pairs& pr, int64_t e) {
 template <class C>
 struct SParams {
     float W1[C::H1 * C::XD];
-    float b1[C::H1];
+    alignas(16) float b1[C::H1];  // read in pairs by the tensor-core forward
     float cw[C::H1 * C::XD];   // W1[n][d] / sd[d]: first-layer tangent along d
     float c2[C::H1 * (C::NS > 0 ? C::NS : 1)];  // per slot s: sum of cw[n][d]^2 over its dims
     // 16-byte aligned: the layer-2 loops read pairs of neighbouring weights
     alignas(16) float W2t[C::TWO ? C::H1 * C::H2 : 4];  // [n][k]
     alignas(16) float W2[C::TWO ? C::H2 * C::H1 : 4];   // [k][n]
     alignas(16) float b2[C::TWO ? C::H2 : 4];
-    float W3[C::HL];
+    alignas(16) float W3[C::HL];
     float b3;
     // activation parameters sigma(z) = c f(o z) of the hidden neurons (adaptive networks)
     float ac1[C::EXTRA > 0 ? C::H1 : 1], ao1[C::EXTRA > 0 ? C::H1 : 1];

@@ -139,6 +139,27 @@ __host__ __device__ constexpr int tc_a_of(int c) {
     return c == 0 ? 0 : (c <= C::XD ? 1 : 2);
 }
 
+// tanh rules of tanh_jet (plain tanh) for two neurons at once in packed FP32
+// pairs: g = [a, tp z_d, tp z_s + tpp sum_d z_d^2] with a = tanh z_0,
+// tp = 1 - a^2, tpp = -2 a tp.
+template <class C>
+__device__ __forceinline__ void tanh_jet_pair(const float2 (&z)[C::J], float2 (&g)[C::J]) {
+    const float2 a = make_float2(tanh_fast(z[0].x), tanh_fast(z[0].y));
+    const float2 tp = fma2(make_float2(-a.x, -a.y), a, dup2(1.0f));
+    const float2 tpp = mul2(mul2(dup2(-2.0f), a), tp);
+    g[0] = a;
+#pragma unroll
+    for (int d = 0; d < C::XD; ++d) g[1 + d] = mul2(tp, z[1 + d]);
+#pragma unroll
+    for (int s = 0; s < C::NS; ++s) {
+        float2 q = dup2(0.f);
+#pragma unroll
+        for (int d = 0; d < C::XD; ++d)
+            if ((C::slot_dims(s) >> d) & 1) q = fma2(z[1 + d], z[1 + d], q);
+        g[1 + C::XD + s] = fma2(tp, z[1 + C::XD + s], mul2(tpp, q));
+    }
+}
+
 // The rest of the jet for one tile on the CUDA cores: this thread's TMEM lane
 // (its pair) of the layer-2 accumulators at taddr -> tanh rules, output layer,
 // unnormalisation, window product -> the pair's record.
@@ -151,21 +172,26 @@ __device__ __forceinline__ void tc_epilogue(const SParams<C>& S, uint32_t taddr,
     for (int c = 0; c < J; ++c) tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), acc[c]);
     tmem_wait_ld();
     if (!act) return;
+    // neurons k, k+1 in packed pairs; the output layer sums even and odd
+    // neurons separately and adds the two at the end
+    float2 o2[J];
+#pragma unroll
+    for (int c = 0; c < J; ++c) o2[c] = dup2(0.f);
+    o2[0].x = S.b3;
+#pragma unroll
+    for (int k = 0; k < H2; k += 2) {
+        float2 z[J], g[J];
+#pragma unroll
+        for (int c = 0; c < J; ++c) z[c] = make_float2(acc[c][k], acc[c][k + 1]);
+        z[0] = add2(z[0], *reinterpret_cast<const float2*>(&S.b2[k]));
+        tanh_jet_pair<C>(z, g);
+        const float2 w3 = *reinterpret_cast<const float2*>(&S.W3[k]);
+#pragma unroll
+        for (int c = 0; c < J; ++c) o2[c] = fma2(w3, g[c], o2[c]);
+    }
     float o[J];
 #pragma unroll
-    for (int c = 0; c < J; ++c) o[c] = 0.f;
-    o[0] = S.b3;
-#pragma unroll
-    for (int k = 0; k < H2; ++k) {
-        float z[J], g[J], a, tp, tpp, tppp;
-#pragma unroll
-        for (int c = 0; c < J; ++c) z[c] = acc[c][k];
-        z[0] += S.b2[k];
-        tanh_jet<C>(z, g, a, tp, tpp, tppp);
-        const float w3 = S.W3[k];
-#pragma unroll
-        for (int c = 0; c < J; ++c) o[c] = fmaf(w3, g[c], o[c]);
-    }
+    for (int c = 0; c < J; ++c) o[c] = o2[c].x + o2[c].y;
     float u[J];
 #pragma unroll
     for (int c = 0; c < J; ++c) u[c] = o[c] * S.sd_u;
@@ -263,25 +289,35 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             for (int d = 0; d < XD; ++d) xn[d] = (xr_n[d] - S.mu[d]) * S.inv_sd[d];
             if (stage) {
                 // this pair's rows of the A operands
+                // (neurons n, n+1 in packed pairs)
 #pragma unroll
                 for (int n4 = 0; n4 < H1; n4 += 4) {
-                    float av[NA][4];
+                    float2 av[NA][2];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        float a, tp, tpp, tppp;
-                        C::AF::derivs(l1_act<C>(S, xn, n4 + q), 1.0f, 1.0f, a, tp, tpp, tppp);
+                    for (int q = 0; q < 2; ++q) {
+                        const int n = n4 + 2 * q;
+                        float2 z = *reinterpret_cast<const float2*>(&S.b1[n]);
+#pragma unroll
+                        for (int d = 0; d < XD; ++d)
+                            z = fma2(make_float2(S.W1[n * XD + d], S.W1[(n + 1) * XD + d]), dup2(xn[d]), z);
+                        const float2 a = make_float2(tanh_fast(z.x), tanh_fast(z.y));
+                        const float2 tp = fma2(make_float2(-a.x, -a.y), a, dup2(1.0f));
                         av[0][q] = a;
                         av[1][q] = tp;
-                        if constexpr (NA > 2) av[NA - 1][q] = tpp;
+                        if constexpr (NA > 2) av[NA - 1][q] = mul2(mul2(dup2(-2.0f), a), tp);
                     }
                     const uint32_t off = kmajor16_off(tid, n4) >> 2;
 #pragma unroll
                     for (int o = 0; o < NA; ++o) {
-                        float h[4], l[4];
+                        float2 h[2], l[2];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) split_tf32(av[o][q], h[q], l[q]);
-                        *reinterpret_cast<float4*>(&T.a[o][0][off]) = make_float4(h[0], h[1], h[2], h[3]);
-                        *reinterpret_cast<float4*>(&T.a[o][1][off]) = make_float4(l[0], l[1], l[2], l[3]);
+                        for (int q = 0; q < 2; ++q) {
+                            h[q] = make_float2(__uint_as_float(__float_as_uint(av[o][q].x) & 0xFFFFE000u),
+                                               __uint_as_float(__float_as_uint(av[o][q].y) & 0xFFFFE000u));
+                            l[q] = add2(av[o][q], make_float2(-h[q].x, -h[q].y));  // v - hi, exact
+                        }
+                        *reinterpret_cast<float4*>(&T.a[o][0][off]) = make_float4(h[0].x, h[0].y, h[1].x, h[1].y);
+                        *reinterpret_cast<float4*>(&T.a[o][1][off]) = make_float4(l[0].x, l[0].y, l[1].x, l[1].y);
                     }
                 }
                 fence_async_smem();

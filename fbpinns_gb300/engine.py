@@ -178,7 +178,7 @@ class PointSet:
                                       _lib.ptr(self.item_start_all), _lib.ptr(self.n_items_all), self.items_cap,
                                       _lib.ptr(t_status(self)), _lib.ptr(self.work_scratch), ws, st),
                    "fbp_build_work")
-        active = (eng.state == 1).to(torch.uint8) if state is None else state
+        active = eng.active if state is None else state
         self.adj_select = active.contiguous()
         _lib.check(lib.fbp_build_work(_lib.ptr(self.sd_start), eng.m, _lib.ptr(self.adj_select), self.chunk,
                                       _lib.ptr(self.items_act), _lib.ptr(self.item_start_act),
@@ -279,6 +279,7 @@ class FBPINNEngine:
         self.m2 = torch.zeros_like(self.theta)
         self.count = torch.zeros(1, dtype=torch.int32, device=dev)
         self.state = torch.ones(self.m, dtype=torch.uint8, device=dev)
+        self.active = torch.ones(self.m, dtype=torch.uint8, device=dev)  # state == 1, the adjoint's selection
         self.grad = torch.zeros_like(self.theta)
         nparts = 8 * torch.cuda.get_device_properties(dev).multi_processor_count + 1
         self.loss_part = torch.zeros(nparts, dtype=torch.float64, device=dev)
@@ -293,6 +294,7 @@ class FBPINNEngine:
     def set_state(self, active):
         """active: (m,) ints, 0 = not trained, 1 = active, 2 = fixed (after get_inputs masking)."""
         self.state.copy_(torch.as_tensor(np.asarray(active), dtype=torch.uint8).to(self.device))
+        self.active.copy_((self.state == 1).to(torch.uint8))
 
     def net_struct(self, theta=None, d2mask=None):
         g = self.grid
