@@ -408,7 +408,7 @@ def run_fused(args, world, rank, local):
                 "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
-                           "parallelism": f"replicas x{world}", "chunk": args.chunk, "forward_chunk": eng.forward_chunk, "schedule": eng.schedule,
+                           "parallelism": f"replicas x{world}", "chunk": step.ps.chunk, "forward_chunk": step.ps.fwd_chunk, "schedule": eng.schedule,
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %

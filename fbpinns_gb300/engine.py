@@ -94,6 +94,11 @@ def record_stride(J):
     return (2 * J + 3) // 4 * 4
 
 
+def _pow2_floor(v):
+    v = max(int(v), 1)
+    return 1 << (v.bit_length() - 1)
+
+
 class PointSet:
     """Interaction lists, subdomain-major pair order, work queues and jet buffers
     of one set of points ``x`` (n, xd) on the device.
@@ -110,8 +115,10 @@ class PointSet:
         self.n = int(x.shape[0])
         self.x = x.to(g.device, torch.float32).contiguous()
         self.J = engine.J
-        self.chunk = int(chunk or engine.chunk)  # pairs per adjoint work item
-        self.fwd_chunk = max(self.chunk, engine.forward_chunk)  # pairs per forward work item
+        # requested pairs per adjoint / forward work item (the sizes used are set
+        # with the buffers: smaller for small pair counts, see _allocate)
+        self.chunk_req = int(chunk or engine.chunk)
+        self.fwd_req = max(self.chunk_req, engine.forward_chunk)
         self.select = select
         s_cap, u_cap = (None, None) if caps is None else caps
         self.takes = PointTakes(g, self.n, s_cap=s_cap, u_cap=u_cap)
@@ -133,6 +140,16 @@ class PointSet:
         lib = _lib.load()
         self.sort_scratch = torch.empty(int(lib.fbp_sort_scratch_bytes(s_cap, m)) // 4 + 1, **i32)
         self.work_scratch = torch.empty(int(lib.fbp_work_scratch_bytes(m)) // 4 + 1, **i32)
+        # Work-item sizes: the requested ones, cut (to powers of two) so that a
+        # small step still gives every SM several adjoint items and a few
+        # forward items; a dynamic schedule only when there are more items than
+        # resident CTAs (otherwise its counter reset costs more than it saves)
+        sms = eng.sm_count
+        self.chunk, self.fwd_chunk = self.chunk_req, self.fwd_req
+        if eng.adaptive_items:
+            self.chunk = min(self.chunk_req, max(128, _pow2_floor(s_cap // (8 * sms))))
+            self.fwd_chunk = min(self.fwd_req, max(self.chunk, _pow2_floor(s_cap // (4 * sms))))
+        self.dynamic = s_cap // self.chunk + m > 4 * sms
         self.items_cap = s_cap // self.chunk + m + 1
         self.forward_items_cap = s_cap // self.fwd_chunk + m + 1  # the forward queue's items fit in this
         self.items_all = torch.zeros(3 * self.items_cap, **i32)
@@ -194,7 +211,7 @@ class PointSet:
             p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
         p.items_cap = self.items_cap
         p.slots_cap = self.slot_out.shape[0]
-        if self.eng.schedule == "dynamic":
+        if self.eng.schedule == "dynamic" and self.dynamic:
             p.item_ctr = _lib.ptr(self.item_ctr[1 if adjoint else 0])
         return p
 
@@ -220,7 +237,7 @@ class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
-                 activation="tanh", schedule="dynamic", forward_chunk=None):
+                 activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -266,6 +283,9 @@ class FBPINNEngine:
         if schedule not in ("dynamic", "static", "per_item"):
             raise ValueError(f"schedule must be 'dynamic', 'static' or 'per_item', not {schedule!r}")
         self.schedule = schedule
+        # cut the work-item sizes for small pair counts (PointSet._allocate)
+        self.adaptive_items = bool(adaptive_items)
+        self.sm_count = torch.cuda.get_device_properties(self.device).multi_processor_count
         # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
         # None = wherever available, True = required, False = CUDA-core FMA kernel
         tc_ok = tc_supported(self.xd, self.h1, self.h2) and self.act == _lib.ACT_TANH
