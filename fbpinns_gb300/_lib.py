@@ -36,9 +36,10 @@ def d2_group(d2):
     return (d2 & 7) if d2 & D2_LAPLACIAN else ((d2 >> 4) & 7 & d2)
 # FBP_ACT_*: hidden-layer activation of the compiled networks, and the number of
 # trainable activation parameters per neuron that each layer adds to W, b
-ACT_TANH, ACT_SIN, ACT_ADAPTIVE_TANH, ACT_ADAPTIVE_SIN = 0, 1, 2, 3
-ACTIVATIONS = {"tanh": ACT_TANH, "sin": ACT_SIN, "adaptive_tanh": ACT_ADAPTIVE_TANH, "adaptive_sin": ACT_ADAPTIVE_SIN}
-ACT_EXTRA = {"tanh": 0, "sin": 0, "adaptive_tanh": 1, "adaptive_sin": 2}
+ACT_TANH, ACT_SIN, ACT_ADAPTIVE_TANH, ACT_ADAPTIVE_SIN, ACT_FOURIER = 0, 1, 2, 3, 4
+ACTIVATIONS = {"tanh": ACT_TANH, "sin": ACT_SIN, "adaptive_tanh": ACT_ADAPTIVE_TANH, "adaptive_sin": ACT_ADAPTIVE_SIN,
+               "fourier": ACT_FOURIER}
+ACT_EXTRA = {"tanh": 0, "sin": 0, "adaptive_tanh": 1, "adaptive_sin": 2, "fourier": 0}
 
 
 class FBPLibraryError(RuntimeError):

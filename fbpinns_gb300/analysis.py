@@ -48,14 +48,16 @@ def _torch_tree(d):
 def FBPINN_solution(c, all_params, active, x_batch):
     """The FBPINN at points x_batch with all subdomains (fbpinns/analysis.py:49-55), on the GPU engine."""
     from .engine import FBPINNEngine, inference_d2mask
-    from .networks import pack_layers
-    from .trainers import FBPINNTrainer, NETWORK_ACTIVATIONS
+    from .networks import pack_layers, engine_network
+    from .trainers import FBPINNTrainer
     ap = _torch_tree(all_params)
-    layers = ap["trainable"]["network"]["subdomain"]["layers"]
-    sizes = [layers[0][0].shape[2]] + [layer[0].shape[1] for layer in layers]
-    act = NETWORK_ACTIVATIONS.get(c.network, "tanh")
+    layers = [tuple(torch.as_tensor(t) for t in layer) for layer in ap["trainable"]["network"]["subdomain"]["layers"]]
+    static = ap["static"].get("network", {}).get("subdomain", {})
+    in_dim = static["omega"].shape[2] if "omega" in static else layers[0][0].shape[2]
+    sizes = [in_dim] + [layer[0].shape[1] for layer in layers]
+    sizes, act, layers, _ = engine_network(c.network, static, layers, sizes)
     eng = FBPINNEngine(ap["static"]["decomposition"], sizes, inference_d2mask(sizes, act), activation=act)
-    eng.set_theta(pack_layers([tuple(torch.as_tensor(t) for t in layer) for layer in layers]))
+    eng.set_theta(pack_layers(layers))
     dev = eng.device
     ap["static"]["problem"] = {k: (v.to(dev) if torch.is_tensor(v) else v) for k, v in ap["static"]["problem"].items()}
     return FBPINNTrainer.predict(eng, ap, c.problem, torch.as_tensor(x_batch, dtype=torch.float32))

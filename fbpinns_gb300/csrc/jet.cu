@@ -7,6 +7,7 @@ int jet_group_b(int, const fbp_net*, const float*, const fbp_pairs*, const float
 int jet_group_c(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 int jet_group_d(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 int jet_group_e(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
+int jet_group_f(int, const fbp_net*, const float*, const fbp_pairs*, const float*, float*, int, cudaStream_t);
 
 static int check_net(const fbp_net* net, const fbp_pairs* pr) {
     FBP_REQUIRE(net && pr, FBP_ERR_INVALID, "jet: null descriptor");
@@ -33,6 +34,8 @@ static int dispatch(int mode, const fbp_net* net, const float* x, const fbp_pair
     r = jet_group_d(mode, net, x, pr, slot_out, out, grid, st);
     if (r != 1) return r;
     r = jet_group_e(mode, net, x, pr, slot_out, out, grid, st);
+    if (r != 1) return r;
+    r = jet_group_f(mode, net, x, pr, slot_out, out, grid, st);
     if (r != 1) return r;
     set_error("jet: no compiled kernel for xd=%d h1=%d h2=%d d2mask=%d act=%d", net->xd, net->h1, net->h2,
               net->d2mask, net->act);
@@ -65,5 +68,6 @@ extern "C" int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask,
     if (r == 1) r = fbp::jet_group_c(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     if (r == 1) r = fbp::jet_group_d(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     if (r == 1) r = fbp::jet_group_e(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
+    if (r == 1) r = fbp::jet_group_f(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr);
     return r == FBP_OK ? 1 : 0;
 }

@@ -101,10 +101,21 @@ __device__ __forceinline__ void act_param_grad(float ab, float d1b, float d2b, f
     }
 }
 
+// FourierFCN: a sin first layer (the frozen feature map) and a tanh second
+// layer; Act<FBP_ACT_FOURIER> is the second layer's rule.
+template <>
+struct Act<FBP_ACT_FOURIER> : Act<FBP_ACT_TANH> {};
+
+// activation of hidden layer 1 / 2 for an activation code
+__host__ __device__ constexpr int act_layer1(int a) { return a == FBP_ACT_FOURIER ? FBP_ACT_SIN : a; }
+__host__ __device__ constexpr int act_layer2(int a) { return a == FBP_ACT_FOURIER ? FBP_ACT_TANH : a; }
+
 template <int XD_, int H1_, int H2_, int D2_, int ACT_ = FBP_ACT_TANH>
 struct Cfg {
     static constexpr int XD = XD_, H1 = H1_, H2 = H2_, D2 = D2_, ACT = ACT_;
-    using AF = Act<ACT_>;
+    using AF = Act<act_layer2(ACT_)>;   // second hidden layer (the only one when H2 = 0)
+    using AF1 = Act<act_layer1(ACT_)>;  // first hidden layer
+    static constexpr bool FROZEN1 = ACT_ == FBP_ACT_FOURIER;  // layer 1 is not trained
     static constexpr int EXTRA = AF::EXTRA;  // per-neuron activation parameters of every layer
     static constexpr int NS = d2_slots(D2);
     static constexpr int J = 1 + XD + NS;
@@ -259,7 +270,7 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
 template <class C>
 __device__ __forceinline__ void l1_jet(const SParams<C>& S, int n, float s, float (&v)[C::J]) {
     float tp, tpp, tppp;
-    C::AF::derivs(s, act_c<C, false>(S, n), act_o<C, false>(S, n), v[0], tp, tpp, tppp);
+    C::AF1::derivs(s, act_c<C, false>(S, n), act_o<C, false>(S, n), v[0], tp, tpp, tppp);
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) v[1 + d] = tp * S.cw[n * C::XD + d];
 #pragma unroll
@@ -406,7 +417,7 @@ __device__ __forceinline__ float l1_act(const SParams<C>& S, const float (&xn)[C
     float z = S.b1[n];
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) z = fmaf(S.W1[n * C::XD + d], xn[d], z);
-    return C::AF::stored(z, act_o<C, false>(S, n));
+    return C::AF1::stored(z, act_o<C, false>(S, n));
 }
 
 // Layer-2 z-jets for neurons [k0, k0+KC) from first-layer activations a1row[n*stride]
@@ -843,7 +854,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                         const int n = n0 + q;
                         const float cn = act_c<C, false>(S, n), on = act_o<C, false>(S, n);
                         float a, tp, tpp, tppp;
-                        C::AF::derivs(a1row[n], cn, on, a, tp, tpp, tppp);
+                        C::AF1::derivs(a1row[n], cn, on, a, tp, tpp, tppp);
                         float tpb = 0.f, tppb = 0.f, cwb[XD];
 #pragma unroll
                         for (int d = 0; d < XD; ++d) {
@@ -905,7 +916,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
 #pragma unroll
                             for (int q = 0; q < A::NB; ++q) {
                                 float a, tp, tpp, tppp;
-                                C::AF::derivs(R.a1[t * A::AS + n0 + q], act_c<C, false>(S, n0 + q),
+                                C::AF1::derivs(R.a1[t * A::AS + n0 + q], act_c<C, false>(S, n0 + q),
                                               act_o<C, false>(S, n0 + q), a, tp, tpp, tppp);
                                 m[q][0] = a;
                                 m[q][1] = tp;
@@ -963,13 +974,13 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             float v = 0.f;
 #pragma unroll
             for (int w = 0; w < NW; ++w) v += RW[w].gW1[i];
-            dst[C::oW1 + i] = v;
+            dst[C::oW1 + i] = C::FROZEN1 ? 0.f : v;
         }
         for (int i = tid; i < H1; i += blockDim.x) {
             float v = 0.f;
 #pragma unroll
             for (int w = 0; w < NW; ++w) v += RW[w].gb1[i];
-            dst[C::ob1 + i] = v;
+            dst[C::ob1 + i] = C::FROZEN1 ? 0.f : v;
         }
         if constexpr (C::TWO) {
             for (int i = tid; i < H2 * H1; i += blockDim.x) {

@@ -137,6 +137,42 @@ class FourierFCN(FCN):
         return FCN.network_fn(params, x)
 
 
+# Network classes with compiled jet kernels, by activation code of the kernels
+NETWORK_ACTIVATIONS = {FCN: "tanh", SIREN: "sin", AdaptiveFCN: "adaptive_tanh", AdaptiveSIREN: "adaptive_sin",
+                       FourierFCN: "fourier"}
+
+
+def fourier_feature_layer(omega):
+    """FourierFCN's feature map as a first layer sin(W x + b) of the kernels:
+    W = [omega; omega], b = [0; pi/2], i.e. [sin(omega x), cos(omega x)]
+    (fbpinns/networks.py:186-188); omega (m, F, xd) -> (W (m, 2F, xd), b (m, 2F))."""
+    omega = torch.as_tensor(omega, dtype=torch.float32)
+    m, F = omega.shape[0], omega.shape[1]
+    W = torch.cat([omega, omega], dim=1)
+    b = torch.cat([torch.zeros((m, F)), torch.full((m, F), math.pi / 2)], dim=1).to(omega.device)
+    return W, b
+
+
+def engine_network(network, static, layers, layer_sizes):
+    """The compiled kernels' view of a network: (layer sizes, activation,
+    layers as packed tuples, leading engine layers that are not trainable).
+    FourierFCN with layer_sizes [xd, h, 1] becomes [xd, 2F, h, 1] with the frozen
+    feature layer first; FourierFCN with more hidden layers has no kernel."""
+    if network not in NETWORK_ACTIVATIONS:
+        raise NotImplementedError("the compiled jet kernels implement the FCN, SIREN, AdaptiveFCN, AdaptiveSIREN "
+                                  "and FourierFCN networks")
+    act = NETWORK_ACTIVATIONS[network]
+    ls = list(layer_sizes)
+    if network is FourierFCN:
+        if len(ls) != 3:
+            raise NotImplementedError("FourierFCN runs in the compiled kernels with one hidden layer after its "
+                                      f"features (layer_sizes [xd, h, 1]), not {ls}")
+        omega = static["omega"]
+        feat = fourier_feature_layer(omega)
+        return [ls[0], 2 * omega.shape[1]] + ls[1:], act, [feat] + list(layers), 1
+    return ls, act, list(layers), 0
+
+
 def norm(mu, sd, x):
     """fbpinns/networks.py:197-198."""
     return (x - mu) / sd

@@ -58,9 +58,11 @@ class PlainStep:
         rows = theta[ids]
         layers = unpack_layers(rows, eng.layer_sizes, eng.extra)
         h = xn
-        for layer in layers[:-1]:
+        for li, layer in enumerate(layers[:-1]):
             z = torch.baddbmm(layer[1][:, None, :], h, layer[0].transpose(1, 2))
-            if eng.activation == "tanh":
+            if eng.activation == "fourier":  # the frozen feature layer, then tanh
+                h = torch.sin(z) if li == 0 else torch.tanh(z)
+            elif eng.activation == "tanh":
                 h = torch.tanh(z)
             elif eng.activation == "sin":
                 h = torch.sin(z)

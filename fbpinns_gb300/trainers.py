@@ -25,10 +25,8 @@ import torch
 
 from . import _lib
 from .engine import FBPINNEngine, FBPINNJet, constrained_jets, d2mask_of, jet_index
-from .networks import fcn_param_count, pack_layers, unpack_layers, FCN, SIREN, AdaptiveFCN, AdaptiveSIREN
-
-# network classes with compiled jet kernels, by hidden-layer activation
-NETWORK_ACTIVATIONS = {FCN: "tanh", SIREN: "sin", AdaptiveFCN: "adaptive_tanh", AdaptiveSIREN: "adaptive_sin"}
+from .networks import (fcn_param_count, pack_layers, unpack_layers, engine_network,  # noqa: F401
+                       NETWORK_ACTIVATIONS, FCN, SIREN, AdaptiveFCN, AdaptiveSIREN, FourierFCN)
 from .optim import adam_update
 from .takes import get_inputs, split_takes, inside_models, grid_of  # noqa: F401  (re-exported API)
 
@@ -322,7 +320,8 @@ def init_subdomain_networks(network, kwargs, m, seed):
     g = torch.Generator().manual_seed(int(seed))
     seeds = torch.randint(0, 2 ** 62, (m,), generator=g).tolist()
     per = [network.init_params(s, **kwargs) for s in seeds]
-    static = per[0][0]
+    # static network parameters are per subdomain too (FourierFCN's omega: (m, F, xd))
+    static = {k: torch.stack([torch.as_tensor(p[0][k]) for p in per]) for k in per[0][0]}
     layers = [tuple(torch.stack([p[1]["layers"][li][k] for p in per]) for k in range(len(per[0][1]["layers"][li])))
               for li in range(len(per[0][1]["layers"]))]
     return static, {"layers": layers}
@@ -366,12 +365,12 @@ class FBPINNTrainer:
         m, xd = st_dec["m"], st_dec["xd"]
         assert all_params["static"]["domain"]["xd"] == all_params["static"]["problem"]["dims"][1] == xd
         logger.info(f"Total number of subdomains: {m}")
-        if c.network not in NETWORK_ACTIVATIONS:
-            raise NotImplementedError("the compiled jet kernels implement the FCN, SIREN, AdaptiveFCN and "
-                                      "AdaptiveSIREN networks")
-        activation = NETWORK_ACTIVATIONS[c.network]
         net_static, net_tr = init_subdomain_networks(c.network, c.network_init_kwargs, m, c.seed)
-        layer_sizes = list(c.network_init_kwargs["layer_sizes"])
+        # the kernels' layers (FourierFCN: its frozen feature layer first)
+        layer_sizes, activation, eng_layers, self.frozen_layers = engine_network(
+            c.network, net_static, net_tr["layers"], c.network_init_kwargs["layer_sizes"])
+        if net_static:  # (model pickles carry them from the start)
+            all_params["static"]["network"] = {"subdomain": net_static}
         scheduler = c.scheduler(all_params=all_params, n_steps=c.n_steps, **c.scheduler_kwargs)
 
         # constraints (sampled once, as the reference does; or resampled per step)
@@ -395,7 +394,7 @@ class FBPINNTrainer:
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
                            tensor_cores=getattr(c, "tensor_cores", None), activation=activation,
                            forward_chunk=getattr(c, "forward_chunk", None))
-        eng.set_theta(pack_layers(net_tr["layers"]))
+        eng.set_theta(pack_layers(eng_layers))
         for k, v in list(all_params["trainable"].get("problem", {}).items()):
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()
         all_params["static"]["problem"] = {k: _to_dev(v, dev) for k, v in all_params["static"]["problem"].items()}
@@ -484,7 +483,8 @@ class FBPINNTrainer:
             torch.cuda.synchronize()
             step.check()
         all_params["trainable"]["network"] = {"subdomain": {"layers": [
-            tuple(t.detach().cpu().clone() for t in layer) for layer in unpack_layers(eng.theta, layer_sizes, eng.extra)]}}
+            tuple(t.detach().cpu().clone() for t in layer)
+            for layer in unpack_layers(eng.theta, layer_sizes, eng.extra)[self.frozen_layers:]]}}
         if net_static:
             all_params["static"]["network"] = {"subdomain": net_static}
         logger.info(f"[i: {c.n_steps}/{c.n_steps}] Training complete")
@@ -504,9 +504,9 @@ class FBPINNTrainer:
     def model_tuple(self, i, eng, all_params):
         """(i, all_params, all_opt_states, active, u_test_losses) as numpy, the
         layout of the reference's model pickles (fbpinns/trainers.py:721)."""
-        ls = list(self.c.network_init_kwargs["layer_sizes"])
+        ls, skip = eng.layer_sizes, getattr(self, "frozen_layers", 0)
         def tree(t):
-            return [tuple(x.cpu().numpy().copy() for x in layer) for layer in unpack_layers(t, ls, eng.extra)]
+            return [tuple(x.cpu().numpy().copy() for x in layer) for layer in unpack_layers(t, ls, eng.extra)[skip:]]
         layers, mu, nu = tree(eng.theta), tree(eng.m1), tree(eng.m2)
         ap = {"static": self._numpy_tree(all_params["static"]),
               "trainable": {"network": {"subdomain": {"layers": layers}},

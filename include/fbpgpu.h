@@ -64,6 +64,11 @@ extern "C" {
 #define FBP_ACT_SIN 1            /* SIREN (fbpinns/networks.py:102-131) */
 #define FBP_ACT_ADAPTIVE_TANH 2  /* AdaptiveFCN a tanh(z/a) (networks.py:70-100); layers (W, b, a) */
 #define FBP_ACT_ADAPTIVE_SIN 3   /* AdaptiveSIREN c sin(o z) (networks.py:133-163); layers (W, b, c, o) */
+/* FourierFCN (networks.py:165-194) with one hidden layer after its features:
+ * the first layer is the feature map, sin with frozen W1 = [omega; omega],
+ * b1 = [0; pi/2] (sin(omega x), cos(omega x)), the second is tanh; the
+ * gradients of W1 and b1 are written as zero. */
+#define FBP_ACT_FOURIER 4
 
 /* Device status word bits (written by kernels into an int32 the caller owns). */
 #define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */

@@ -106,11 +106,19 @@ def fcn(layers, x, activation="tanh"):
     """The reference's networks batched over pairs: W (s,fo,fi), b (s,fo) and the
     layer's activation parameters (s,fo): FCN tanh (``fbpinns/networks.py:61-68``),
     SIREN sin (``:102-131``), AdaptiveFCN a tanh(x/a) (``:70-100``), AdaptiveSIREN
-    c sin(o x) (``:133-163``)."""
-    for layer in layers[:-1]:
+    c sin(o x) (``:133-163``).  FourierFCN (``:165-194``, activation "fourier"):
+    the first layer holds its features as W = [omega; omega] (the engine's
+    packing); the oracle reads omega from the first half of the rows and
+    computes [sin(omega x), cos(omega x)] as the reference does, then tanh layers."""
+    for li, layer in enumerate(layers[:-1]):
         w, b = layer[0], layer[1]
+        if activation == "fourier" and li == 0:
+            F = w.shape[1] // 2
+            z = torch.einsum("sij,sj->si", w[:, :F], x)
+            x = torch.cat([torch.sin(z), torch.cos(z)], dim=1)
+            continue
         x = torch.einsum("sij,sj->si", w, x) + b
-        if activation == "tanh":
+        if activation == "tanh" or activation == "fourier":
             x = torch.tanh(x)
         elif activation == "sin":
             x = torch.sin(x)

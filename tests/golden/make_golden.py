@@ -210,11 +210,17 @@ def main():
         dmax = np.min(np.abs(xb[:, None, :] - xmaxs[None]), axis=(1, 2))
         return (dmin > margin) & (dmax > margin)
 
-    def model_case(tag, decomp, sp_params, problem, pkw, layer_sizes, xb, seed, dims, network="FCN", wscale=1.0):
+    def model_case(tag, decomp, sp_params, problem, pkw, layer_sizes, xb, seed, dims, network="FCN", wscale=1.0,
+                   n_features=0):
         r = np.random.default_rng(seed)
         ps_prob = problem.init_params(**pkw)[0]
         m = sp_params["m"]
         layers = []
+        net_static = {}
+        if network == "FourierFCN":  # per-subdomain omega, 2 pi (mu + sd N(0,1)) with mu = 0, sd = 0.5
+            omega = jnp.array(2 * np.pi * 0.5 * r.normal(size=(m, n_features, layer_sizes[0])))
+            net_static = {"omega": omega}
+            layer_sizes = [2 * n_features] + list(layer_sizes)[1:]
         for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
             v = wscale * np.sqrt(1 / fi)
             layer = (jnp.array(r.uniform(-v, v, (m, fo, fi))), jnp.array(r.uniform(-v, v, (m, fo))))
@@ -227,6 +233,8 @@ def main():
         xb = xb[keep].astype(np.float64)
         all_params = {"static": {"decomposition": sp_params, "problem": ps_prob},
                       "trainable": {"network": {"subdomain": {"layers": layers}}}}
+        if net_static:
+            all_params["static"]["network"] = {"subdomain": net_static}
         active = np.ones(m, dtype=int)
         takes, all_ims, (_, _, _, cut_all, _) = trainers.get_inputs(jnp.array(xb), active, all_params, decomp)
         apc = {"static": cut_all(all_params["static"]), "trainable": cut_all(all_params["trainable"])}
@@ -242,6 +250,8 @@ def main():
         arrays = dict(x_batch=xb, m_take=takes[0], n_take=takes[1], p_take=takes[2], np_take=takes[3],
                       npou=takes[4], all_ims=all_ims, u=u, wp=wp, us=us, ws=ws, us_raw=ur,
                       u_raw=ufun_raw(xb))
+        if net_static:
+            arrays["omega"] = net_static["omega"]
         for i, layer in enumerate(layers):
             arrays[f"W{i}"] = layer[0]
             arrays[f"b{i}"] = layer[1]
@@ -299,6 +309,14 @@ def main():
     loss_fns["multilevel_adasiren"] = loss_fns["multilevel"]
     model_case("multilevel_adasiren", DM, spm, BU, dict(), [2, 8, 8, 1], rng_a.uniform(0, 1, (600, 2)), 20,
                [0, 1], network="AdaptiveSIREN", wscale=np.sqrt(6.0))
+    # FourierFCN (networks.py:165-194): 4 features, one hidden layer of 8
+    rng_f = np.random.default_rng(93)
+    loss_fns["ho_hardbc_fourier"] = loss_fns["ho_hardbc"]
+    model_case("ho_hardbc_fourier", D, sp, HOH, dict(d=2, w0=80, sd=0.1), [1, 8, 1], xho, 21, [0],
+               network="FourierFCN", n_features=4)
+    loss_fns["multilevel_fourier"] = loss_fns["multilevel"]
+    model_case("multilevel_fourier", DM, spm, BU, dict(), [2, 8, 1], rng_f.uniform(0, 1, (600, 2)), 22, [0, 1],
+               network="FourierFCN", n_features=4)
 
     # constraining functions and losses on given jets
     xc = rng.uniform([-1, -1, 0], [1, 1, 1], (64, 3))

@@ -1,6 +1,8 @@
 """Shared builders for the parity tests: the same decomposition, weights and
 points for the CUDA engine (float32) and the CPU oracle (float64)."""
 
+import math
+
 import numpy as np
 import torch
 
@@ -44,8 +46,15 @@ def boxes_static(xmin, xmax, pou=None):
 
 
 def golden_layers(g):
-    """Layer tuples (W, b[, a] or [, c, o]) of a golden model fixture."""
+    """Layer tuples (W, b[, a] or [, c, o]) of a golden model fixture; for a
+    FourierFCN fixture (``omega`` saved) the frozen feature layer
+    (W = [omega; omega], b = [0; pi/2]) comes first, as the engine packs it."""
     out, i = [], 0
+    if "omega" in g:
+        om = torch.tensor(g["omega"])
+        m, F = om.shape[0], om.shape[1]
+        out.append((torch.cat([om, om], 1),
+                    torch.cat([torch.zeros((m, F), dtype=om.dtype), torch.full((m, F), math.pi / 2, dtype=om.dtype)], 1)))
     while f"W{i}" in g:
         layer = [torch.tensor(g[f"W{i}"]), torch.tensor(g[f"b{i}"])]
         layer += [torch.tensor(g[f"{k}{i}"]) for k in "AO" if f"{k}{i}" in g]
@@ -54,11 +63,11 @@ def golden_layers(g):
     return out
 
 
-GOLDEN_ACTIVATION = {"siren": "sin", "adafcn": "adaptive_tanh", "adasiren": "adaptive_sin"}
+GOLDEN_ACTIVATION = {"siren": "sin", "adafcn": "adaptive_tanh", "adasiren": "adaptive_sin", "fourier": "fourier"}
 
 
 def golden_activation(tag):
-    """Activation of a golden model tag (suffix _siren, _adafcn, _adasiren; else tanh)."""
+    """Activation of a golden model tag (suffix _siren, _adafcn, _adasiren, _fourier; else tanh)."""
     return GOLDEN_ACTIVATION.get(tag.rsplit("_", 1)[-1], "tanh")
 
 

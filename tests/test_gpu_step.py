@@ -39,11 +39,12 @@ def _engine(static, layers, d2mask, chunk=64, activation="tanh"):
                                          ("multilevel", [0, 1], 3), ("ho_hardbc_siren", [0], 1),
                                          ("multilevel_siren", [0, 1], 3), ("ho_hardbc_adafcn", [0], 1),
                                          ("multilevel_adafcn", [0, 1], 3), ("ho_hardbc_adasiren", [0], 1),
-                                         ("multilevel_adasiren", [0, 1], 3)])
+                                         ("multilevel_adasiren", [0, 1], 3), ("ho_hardbc_fourier", [0], 1),
+                                         ("multilevel_fourier", [0, 1], 3)])
 def test_jets_vs_reference_golden(cuda, tag, dims, d2):
     """POU-combined network jets (before the constraint) vs the reference's
     forward values and their float64 finite differences (FCN, SIREN,
-    AdaptiveFCN, AdaptiveSIREN)."""
+    AdaptiveFCN, AdaptiveSIREN, FourierFCN)."""
     g = golden(f"model_{tag}.npz")
     static = decomposition(golden_base(tag))
     layers = golden_layers(g)
@@ -173,6 +174,45 @@ def test_network_fused_loss_and_gradient_vs_oracle(cuda, name, lap, act):
     ps.check_status()
     assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
     assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
+
+
+@pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("poisson", False), ("poisson", True)])
+def test_fourier_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
+    """FourierFCN (4 features, one hidden layer of 8): fused loss and the
+    gradients of the trainable layers vs the float64 oracle, which computes
+    [sin(omega x), cos(omega x)] as the reference does; the frozen feature
+    layer's gradient is exactly zero."""
+    from fbpinns_gb300.networks import fourier_feature_layer
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    static = decomposition(recipe)
+    m, xd = static["m"], ls[0]
+    gen = torch.Generator().manual_seed(83)
+    omega = (2 * math.pi * 0.5 * torch.randn((m, 4, xd), generator=gen, dtype=torch.float64)).float()
+    feat = tuple(t.double() for t in fourier_feature_layer(omega))
+    layers32 = [feat] + [tuple(t.float().double() for t in layer) for layer in random_layers([8, 8, 1], m, seed=9)]
+    x = _points(recipe if recipe != "multilevel" else "poisson", 500, 29)
+    prob_static = pcls.init_params(**pkw)[0]
+    P = oracle_params(static, layers32, opar)
+    P["activation"] = "fourier"
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(m, dtype=int), p[0].numpy(),
+                                                          p[1].numpy(), static["subdomain"]["pou"].numpy())
+    loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
+                                           [OM.get_jmaps(_required(name))], ocls)
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for layer in grads[1:] for t in layer], 1).numpy()
+    eng = _engine(static, layers32, d2 | (_lib.D2_LAPLACIAN if lap else 0), activation="fourier")
+    assert eng.layer_sizes == [xd, 8, 8, 1]
+    eng.set_state(active)
+    eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+    ps = eng.points(torch.tensor(x))
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    n_feat = 8 * xd + 8  # W1 and b1 of the feature layer
+    assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
+    assert np.all(grad[:, :n_feat] == 0)
+    assert rel_err(grad[a_ims][:, n_feat:], g_ref) < GRAD_TOL
 
 
 def test_laplacian_jets_match_sum_of_second_derivatives(cuda):

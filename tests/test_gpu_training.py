@@ -109,3 +109,36 @@ def test_adaptive_networks_train_fused(cuda, netname):
     layers = ap["trainable"]["network"]["subdomain"]["layers"]
     assert all(len(layer) == (3 if netname == "AdaptiveFCN" else 4) for layer in layers)
     assert not torch.allclose(layers[0][2], torch.ones_like(layers[0][2]))
+
+
+def test_fourier_network_trains_fused_and_reloads(cuda, tmp_path, monkeypatch):
+    """FourierFCN (networks.py:165-194; 8 features, one hidden layer of 32)
+    through the fused engine: the HO problem trains, omega stays as it was
+    drawn, the returned and saved params keep the reference's layout
+    (static omega (m, F, xd), trainable [(W (m,32,16), b), (W (m,1,32), b)])
+    and inference from the saved model agrees with the live engine."""
+    from fbpinns_gb300.analysis import load_model, FBPINN_solution
+    from fbpinns_gb300.networks import FourierFCN
+    monkeypatch.chdir(tmp_path)
+    c = configs.ho(n_steps=150)
+    c.network = FourierFCN
+    c.network_init_kwargs = dict(layer_sizes=[1, 32, 1], mu=0.0, sd=1.0, n_features=8)
+    c.run = "fourier"
+    c.save_models, c.model_save_freq = True, 150
+    c.summary_freq, c.test_freq = 50, 150
+    tr = FBPINNTrainer(c)
+    ap = tr.train()
+    assert tr.engine.activation == "fourier" and tr.engine.layer_sizes == [1, 16, 32, 1]
+    losses = [h["loss"] for h in tr.history]
+    assert all(math.isfinite(v) for v in losses) and losses[-1] < losses[0]
+    omega = ap["static"]["network"]["subdomain"]["omega"]
+    assert tuple(omega.shape) == (15, 8, 1)
+    W1 = tr.engine.theta[:, :16].reshape(15, 16, 1).cpu()
+    assert torch.equal(W1[:, :8], omega.float()) and torch.equal(W1[:, 8:], omega.float())
+    layers = ap["trainable"]["network"]["subdomain"]["layers"]
+    assert [tuple(layer[0].shape) for layer in layers] == [(15, 32, 16), (15, 1, 32)]
+    c2, model = load_model("fourier", rootdir="results/")
+    x = torch.linspace(0, 1, 50).reshape(-1, 1)
+    u_loaded = FBPINN_solution(c2, model[1], model[3], x)
+    u_live = FBPINNTrainer.predict(tr.engine, tr.all_params, c.problem, x)
+    assert torch.allclose(u_loaded, u_live, rtol=1e-6, atol=1e-6)

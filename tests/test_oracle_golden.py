@@ -128,10 +128,10 @@ PROBLEMS = {
              [0, 1, 2]),
     "multilevel": (OP.BurgersEquation2D, {"sd": 0.1, "nu": 0.01 / np.pi}, [0, 1]),
 }
-for _net in ("siren", "adafcn", "adasiren"):  # SIREN, AdaptiveFCN, AdaptiveSIREN (networks.py:70-163)
+for _net in ("siren", "adafcn", "adasiren", "fourier"):  # SIREN, AdaptiveFCN, AdaptiveSIREN, FourierFCN
     PROBLEMS[f"ho_hardbc_{_net}"] = PROBLEMS["ho_hardbc"]
     PROBLEMS[f"multilevel_{_net}"] = PROBLEMS["multilevel"]
-NET_TAGS = [f"{b}_{n}" for n in ("siren", "adafcn", "adasiren") for b in ("ho_hardbc", "multilevel")]
+NET_TAGS = [f"{b}_{n}" for n in ("siren", "adafcn", "adasiren", "fourier") for b in ("ho_hardbc", "multilevel")]
 
 
 @pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "multilevel"] + NET_TAGS)
@@ -172,7 +172,7 @@ def test_model_jets_match_reference_fd(tag):
 
 
 @pytest.mark.parametrize("tag", ["ho_hardbc", "burgers", "wave", "ho_hardbc_siren", "ho_hardbc_adafcn",
-                                 "ho_hardbc_adasiren"])
+                                 "ho_hardbc_adasiren", "ho_hardbc_fourier"])
 def test_loss_matches_reference(tag):
     g = golden(f"model_{tag}.npz")
     prob, pp, dims = PROBLEMS[tag]
@@ -183,6 +183,7 @@ def test_loss_matches_reference(tag):
     req = {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))), "ho_hardbc_siren": ((0, ()), (0, (0,)), (0, (0, 0))),
            "ho_hardbc_adafcn": ((0, ()), (0, (0,)), (0, (0, 0))),
            "ho_hardbc_adasiren": ((0, ()), (0, (0,)), (0, (0, 0))),
+           "ho_hardbc_fourier": ((0, ()), (0, (0,)), (0, (0, 0))),
            "burgers": ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0))),
            "wave": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2)))}[tag]
     loss = OM.fbpinn_loss(P, [[x]], [takes], [OM.get_jmaps(req)], prob)
