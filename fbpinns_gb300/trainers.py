@@ -190,7 +190,8 @@ class FusedStep:
             self.cur = 0
             self.started = False
             self.snap = torch.zeros(1, dtype=torch.int32, device=dev)  # count at the step's start
-            # higher priority: the list kernels take SMs ahead of the persistent adjoint's CTAs
+            # higher priority (kept inside the graphs, see StepGraph): as CTAs of the step's
+            # kernels retire, the block scheduler starts the list kernels' CTAs first
             self.side = torch.cuda.Stream(device=dev, priority=-1)
             self.graphs = [None, None]
             if resample is not None:
