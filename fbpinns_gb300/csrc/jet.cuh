@@ -576,6 +576,13 @@ __host__ __device__ constexpr int pow2_at_least(int v) {
     return p;
 }
 
+#ifndef FBP_ADJ_KB
+#define FBP_ADJ_KB 4  // rows of a lane's W2-bar block (2, 4 or 8)
+#endif
+#ifndef FBP_ADJ_UNROLL_C
+#define FBP_ADJ_UNROLL_C 4  // pairs of the tile per unrolled step of the W2-bar loop
+#endif
+
 template <class C>
 struct AdjW {
     static constexpr int ZS = ((C::HL * C::J + 7) / 8) * 8 + 4;   // z2-bar row stride (floats): 16-B rows,
@@ -583,10 +590,13 @@ struct AdjW {
     static constexpr int AS = C::H1 + 1;                          // a1 row stride
     static constexpr int W = ZS <= 96 ? 4 : 2;                    // warps per CTA
     static constexpr int T = 32 * W;
-    static constexpr int KB = 4, NB = 2;                          // W2-bar block per lane
+    // W2-bar block per lane: KB rows x NB columns (KB x NB = 8); the sums do
+    // not depend on the blocking (each entry adds its pairs in tile order)
+    static constexpr int KB = FBP_ADJ_KB, NB = 8 / FBP_ADJ_KB;
     static constexpr int NBLK = C::TWO ? (C::H2 / KB) * (C::H1 / NB) : 0;
     static constexpr int PASSES = C::TWO ? (NBLK + 31) / 32 : 0;
     static_assert(!C::TWO || (C::H2 % KB == 0 && C::H1 % NB == 0), "W2 blocking");
+    static_assert(KB == 2 || KB == 4 || KB == 8, "W2-bar rows per lane");
 };
 
 // One warp's rows; 16-byte aligned so that every warp's z2-bar rows (read and
@@ -909,8 +919,11 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             for (int q = 0; q < A::NB; ++q)
 #pragma unroll
                                 for (int c = 0; c < J; ++c) sacc[i][q][c] = make_float2(0.f, 0.f);
-                        float b2s[A::KB] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 2
+                        float b2s[A::KB];
+#pragma unroll
+                        for (int i = 0; i < A::KB; ++i) b2s[i] = 0.f;
+                        constexpr int UC = FBP_ADJ_UNROLL_C;
+#pragma unroll UC
                         for (int t = 0; t < nt; ++t) {
                             float m[A::NB][3];
 #pragma unroll
@@ -925,19 +938,30 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             const float* zr = &R.zb[t * A::ZS + k0];
 #pragma unroll
                             for (int c = 0; c < J; ++c) {
-                                const float4 z4 = *reinterpret_cast<const float4*>(zr + c * H2);
+                                float2 z2[A::KB / 2];  // rows k0 .. k0+KB of z2-bar component c
+                                if constexpr (A::KB == 2) {
+                                    z2[0] = *reinterpret_cast<const float2*>(zr + c * H2);
+                                } else {
+#pragma unroll
+                                    for (int h = 0; h < A::KB / 4; ++h) {
+                                        const float4 z4 = *reinterpret_cast<const float4*>(zr + c * H2 + 4 * h);
+                                        z2[2 * h] = make_float2(z4.x, z4.y);
+                                        z2[2 * h + 1] = make_float2(z4.z, z4.w);
+                                    }
+                                }
                                 const int mi = c == 0 ? 0 : (c <= XD ? 1 : 2);
                                 if (c == 0) {
-                                    b2s[0] += z4.x;
-                                    b2s[1] += z4.y;
-                                    b2s[2] += z4.z;
-                                    b2s[3] += z4.w;
+#pragma unroll
+                                    for (int i = 0; i < A::KB / 2; ++i) {
+                                        b2s[2 * i] += z2[i].x;
+                                        b2s[2 * i + 1] += z2[i].y;
+                                    }
                                 }
 #pragma unroll
                                 for (int q = 0; q < A::NB; ++q) {
                                     const float2 mm = make_float2(m[q][mi], m[q][mi]);
-                                    sacc[0][q][c] = fma2(make_float2(z4.x, z4.y), mm, sacc[0][q][c]);
-                                    sacc[1][q][c] = fma2(make_float2(z4.z, z4.w), mm, sacc[1][q][c]);
+#pragma unroll
+                                    for (int i = 0; i < A::KB / 2; ++i) sacc[i][q][c] = fma2(z2[i], mm, sacc[i][q][c]);
                                 }
                             }
                         }
