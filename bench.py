@@ -419,6 +419,100 @@ def run_fused(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_extras(args):
+    """Measurements of the paths either side of the step, on the same Poisson
+    workload (one JSON line; not part of the default run):
+      * the fused step with the other compiled networks (SIREN, AdaptiveFCN,
+        AdaptiveSIREN with 16-16 hidden layers, FourierFCN with 8 features and
+        one hidden layer of 32), steps/s;
+      * test-step inference (forward jets + POU combination at every point of
+        a fixed 2^18-point set, all subdomains): points/s;
+      * the interaction lists rebuilt on the device after a scheduler change
+        (work queues for a new active set, no host synchronisation): ms."""
+    from fbpinns_gb300 import _lib
+    from fbpinns_gb300.engine import FBPINNEngine
+    from fbpinns_gb300.optim import adam
+    from fbpinns_gb300.trainers import FusedStep, init_subdomain_networks
+    from fbpinns_gb300 import networks as NW
+    dev = torch.device("cuda", 0)
+    static = decomposition_static()
+    m = static["m"]
+    problem, all_params = problem_setup()
+    spec = problem.fused_spec(all_params)
+    d2 = 3 | _lib.D2_LAPLACIAN
+    out = {"metric": "extras", "workload": WORKLOAD, "networks": {}}
+
+    def timed_steps(step, k):
+        for _ in range(3):
+            step.step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(k):
+            step.step()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    nets = [("SIREN", NW.SIREN, {"layer_sizes": LAYERS}), ("AdaptiveFCN", NW.AdaptiveFCN, {"layer_sizes": LAYERS}),
+            ("AdaptiveSIREN", NW.AdaptiveSIREN, {"layer_sizes": LAYERS}),
+            ("FourierFCN", NW.FourierFCN, {"layer_sizes": [2, 32, 1], "mu": 0.0, "sd": 1.0, "n_features": 8})]
+    for name, cls, kw in nets:
+        st_, tr = init_subdomain_networks(cls, kw, m, SEED)
+        ls, act, layers, _ = NW.engine_network(cls, st_, tr["layers"], kw["layer_sizes"])
+        eng = FBPINNEngine(static, ls, d2mask=d2, device=dev, activation=act)
+        eng.set_theta(NW.pack_layers(layers))
+        step = FusedStep(eng, spec, adam(LR), resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], SEED), use_graph=True)
+        ms = timed_steps(step, max(args.steps, 10))
+        step.check()
+        out["networks"][name] = {"layers": ls, "activation": act, "ms_per_step": ms, "steps_per_s": 1000.0 / ms}
+        del step, eng
+    # inference on a fixed point set (the test step)
+    eng = FBPINNEngine(static, LAYERS, d2mask=0, device=dev)
+    eng.set_theta(init_theta(m))
+    g = torch.Generator(device="cpu").manual_seed(SEED)
+    xt = torch.rand((N_POINTS, 2), generator=g).to(dev)
+    ps = eng.points(xt)
+    for _ in range(3):
+        eng.forward_pairs(ps)
+        eng.pou_forward(ps)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = 20
+    a.record()
+    for _ in range(k):
+        eng.forward_pairs(ps)
+        eng.pou_forward(ps)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / k
+    out["inference"] = {"points": N_POINTS, "pairs": ps.s, "jet": "u, grad u", "forward_kernel":
+                        "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma", "ms": ms,
+                        "points_per_s": N_POINTS / (ms * 1e-3)}
+    # scheduler change: a new active set -> work queues rebuilt on the device
+    eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev)
+    eng2.set_theta(init_theta(m))
+    ps2 = eng2.points(xt)
+    masks = [np.where(np.arange(m) % 2 == i, 1, 2) for i in range(2)]
+    times = []
+    for i in range(12):
+        eng2.set_state(masks[i % 2])
+        torch.cuda.synchronize()
+        a.record()
+        ps2.build_work()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    out["scheduler_change"] = {"ms_median": float(np.median(times[2:])), "what": "work queues of a new active set "
+                               "(forward: all subdomains with pairs; adjoint: the active ones), on the device"}
+    a.record()
+    ps2.rebuild()
+    b.record()
+    torch.cuda.synchronize()
+    out["list_rebuild_ms"] = a.elapsed_time(b)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,7 +532,12 @@ def main():
     ap.add_argument("--only-timed", action="store_true",
                     help="run only the warm-up and timed fused steps (for profiler launch lists)")
     ap.add_argument("--points", type=int, default=N_POINTS, help="collocation points per step")
+    ap.add_argument("--extras", action="store_true",
+                    help="instead of the bench line: other networks, inference and scheduler-change timings")
     args = ap.parse_args()
+    if args.extras:
+        run_extras(args)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
