@@ -591,8 +591,11 @@ struct AdjW {
     static constexpr int W = ZS <= 96 ? 4 : 2;                    // warps per CTA
     static constexpr int T = 32 * W;
     // W2-bar block per lane: KB rows x NB columns (KB x NB = 8); the sums do
-    // not depend on the blocking (each entry adds its pairs in tile order)
-    static constexpr int KB = FBP_ADJ_KB, NB = 8 / FBP_ADJ_KB;
+    // not depend on the blocking (each entry adds its pairs in tile order).
+    // Activations other than the plain tanh recover sigma, sigma', sigma'' of
+    // the block's columns from z with sin/cos or tanh calls per pair, so they
+    // take one column (8 x 1)
+    static constexpr int KB = C::ACT == FBP_ACT_TANH ? FBP_ADJ_KB : 8, NB = 8 / KB;
     static constexpr int NBLK = C::TWO ? (C::H2 / KB) * (C::H1 / NB) : 0;
     static constexpr int PASSES = C::TWO ? (NBLK + 31) / 32 : 0;
     static_assert(!C::TWO || (C::H2 % KB == 0 && C::H1 % NB == 0), "W2 blocking");
