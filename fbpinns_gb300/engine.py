@@ -99,6 +99,19 @@ def _pow2_floor(v):
     return 1 << (v.bit_length() - 1)
 
 
+def work_item_sizes(s_cap, m, sms, chunk, forward_chunk, adaptive=True):
+    """(adjoint pairs per item, forward pairs per item, counter schedule?) for
+    up to s_cap pairs over m subdomains on sms SMs.  The requested sizes are
+    cut to powers of two (at least 128) so that a small step still gives
+    every SM about 8 adjoint and 4 forward items; the counter-based schedule
+    pays only with more items than resident CTAs (4 per SM)."""
+    adj, fwd = int(chunk), max(int(chunk), int(forward_chunk))
+    if adaptive:
+        adj = min(adj, max(128, _pow2_floor(s_cap // (8 * sms))))
+        fwd = min(fwd, max(adj, _pow2_floor(s_cap // (4 * sms))))
+    return adj, fwd, s_cap // adj + m > 4 * sms
+
+
 class PointSet:
     """Interaction lists, subdomain-major pair order, work queues and jet buffers
     of one set of points ``x`` (n, xd) on the device.
@@ -144,12 +157,8 @@ class PointSet:
         # small step still gives every SM several adjoint items and a few
         # forward items; a dynamic schedule only when there are more items than
         # resident CTAs (otherwise its counter reset costs more than it saves)
-        sms = eng.sm_count
-        self.chunk, self.fwd_chunk = self.chunk_req, self.fwd_req
-        if eng.adaptive_items:
-            self.chunk = min(self.chunk_req, max(128, _pow2_floor(s_cap // (8 * sms))))
-            self.fwd_chunk = min(self.fwd_req, max(self.chunk, _pow2_floor(s_cap // (4 * sms))))
-        self.dynamic = s_cap // self.chunk + m > 4 * sms
+        self.chunk, self.fwd_chunk, self.dynamic = work_item_sizes(s_cap, m, eng.sm_count, self.chunk_req,
+                                                                   self.fwd_req, eng.adaptive_items)
         self.items_cap = s_cap // self.chunk + m + 1
         self.forward_items_cap = s_cap // self.fwd_chunk + m + 1  # the forward queue's items fit in this
         self.items_all = torch.zeros(3 * self.items_cap, **i32)

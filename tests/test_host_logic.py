@@ -277,3 +277,52 @@ def test_required_ujs_mapping():
         d2mask_of([((0, (0, 1)),)], 2)
     with pytest.raises(NotImplementedError):
         d2mask_of([((0, (0, 0, 0)),)], 1)
+
+
+def test_work_item_sizes():
+    """Adjoint/forward work-item sizes and the schedule choice: the requested
+    1024/4096 pairs for the 2D Poisson bench (9.4e6 pairs on 152 SMs), powers
+    of two cut for small steps, and the counter schedule only with more items
+    than resident CTAs."""
+    from fbpinns_gb300.engine import work_item_sizes
+    assert work_item_sizes(11_711_911, 1365, 152, 1024, 4096) == (1024, 4096, True)
+    adj, fwd, dyn = work_item_sizes(314_672, 128, 152, 1024, 4096)  # Burgers
+    assert (adj, fwd, dyn) == (256, 512, True)
+    assert work_item_sizes(398, 15, 152, 1024, 4096) == (128, 128, False)  # HO: 15 items
+    assert work_item_sizes(314_672, 128, 152, 1024, 4096, adaptive=False) == (1024, 4096, False)
+    for s in (10, 10_000, 10_000_000):
+        adj, fwd, _ = work_item_sizes(s, 100, 152, 1024, 4096)
+        assert adj & (adj - 1) == 0 and fwd & (fwd - 1) == 0 and 128 <= adj <= fwd <= 4096
+
+
+def test_fourier_network_maps_to_a_frozen_sin_layer():
+    """FourierFCN (fbpinns/networks.py:165-194) as the kernels see it: a first
+    layer sin(W x + b) with W = [omega; omega], b = [0; pi/2] ahead of the
+    reference's FCN layers; the oracle's "fourier" network (sin and cos of
+    omega x) equals the reference network_fn restated in networks.py, and the
+    packed layer equals it to FP32 rounding; more hidden layers are refused."""
+    from oracle import model as OM
+    g = torch.Generator().manual_seed(3)
+    m, F, xd, h = 5, 4, 2, 8
+    st, tr = N.FourierFCN.init_params(11, [xd, h, 1], 0.0, 1.0, F)
+    omega = torch.stack([st["omega"]] * m)
+    layers = [tuple(torch.stack([t] * m) for t in layer) for layer in tr["layers"]]
+    ls, act, eng_layers, skip = N.engine_network(N.FourierFCN, {"omega": omega}, layers, [xd, h, 1])
+    assert ls == [xd, 2 * F, h, 1] and act == "fourier" and skip == 1 and len(eng_layers) == 3
+    W, b = eng_layers[0]
+    assert torch.equal(W[:, :F], omega) and torch.equal(W[:, F:], omega)
+    assert torch.equal(b[:, :F], torch.zeros(m, F)) and torch.allclose(b[:, F:], torch.full((m, F), math.pi / 2))
+    x = torch.rand((m, xd), generator=g, dtype=torch.float64)
+    L64 = [tuple(t.double() for t in layer) for layer in eng_layers]
+    ref = torch.stack([N.FourierFCN.network_fn({"static": {"network": {"subdomain": {"omega": omega[i].double()}}},
+                                                "trainable": {"network": {"subdomain": {"layers": [
+                                                    tuple(t[i].double() for t in layer) for layer in layers]}}}},
+                                               x[i]) for i in range(m)])
+    assert torch.allclose(OM.fcn(L64, x, "fourier"), ref, rtol=0, atol=1e-12)
+    # the packed form (sin(z + pi/2) for cos z) agrees to the rounding of the FP32 bias
+    z = torch.einsum("sij,sj->si", L64[0][0], x) + L64[0][1]
+    hh = torch.tanh(torch.einsum("sij,sj->si", L64[1][0], torch.sin(z)) + L64[1][1])
+    packed = torch.einsum("sij,sj->si", L64[2][0], hh) + L64[2][1]
+    assert torch.allclose(packed, ref, rtol=0, atol=1e-6)
+    with pytest.raises(NotImplementedError):
+        N.engine_network(N.FourierFCN, {"omega": omega}, layers, [xd, h, h, 1])
