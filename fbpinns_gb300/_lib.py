@@ -106,6 +106,7 @@ _SIG = {
     "fbp_fma_probe": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_double), _P]),
     "fbp_tanh_probe": (C.c_int, [_P, _P, _I64, _P]),
     "fbp_has_shape": (C.c_int, [_I32, _I32, _I32, _I32, _I32]),
+    "fbp_has_tc_shape": (C.c_int, [_I32, _I32, _I32, _I32, _I32]),
 }
 
 _lib = None

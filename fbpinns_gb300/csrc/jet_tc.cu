@@ -1,63 +1,21 @@
 // C ABI of the tensor-core forward jet kernel (tcgen05, 3xTF32) for networks
-// with two 16-wide hidden layers.
-#include <algorithm>
-
-#include "jet_tc.cuh"
+// with two 16-wide hidden layers: the plain tanh FCN here, the other
+// activations in jet_tc_act.cu.
+#include "jet_tc_launch.cuh"
 
 namespace fbp {
+int tc_group_act(int mode, const fbp_net* net, const float* x, const fbp_pairs* pr, float* pair_out,
+                 int32_t* status, int grid, cudaStream_t st);
 
-template <int XD, int D2>
-static int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs& pr, float* pair_out,
-                             int32_t* status, int grid, cudaStream_t st) {
-    using C = Cfg<XD, 16, 16, D2>;
-    FBP_REQUIRE(net.nparam == C::P, FBP_ERR_INVALID, "forward_tc: nparam %d != %d for this shape", net.nparam, C::P);
-    struct Launch {
-        int res;     // resident CTAs per SM
-        size_t shm;  // dynamic shared memory per CTA
-    };
-    static Launch launch_dev[FBP_MAX_DEVICES] = {};  // per device
-    const int dev = current_device();
-    Launch& L = launch_dev[dev];
-    constexpr int cols = TcSmem<C>::COLS;
-    if (!L.res) {
-        size_t shm = sizeof(TcSmem<C>);
-        FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)shm));
-        // CTAs that fit on one SM by shared memory, registers and threads: an
-        // upper bound on how many can be resident at once
-        cudaFuncAttributes fa;
-        FBP_CUDA_CHECK(cudaFuncGetAttributes(&fa, forward_pairs_tc_kernel<C>));
-        int smem_sm = 0, regs_sm = 0, thr_sm = 0;
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
-        const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the driver's 1 KiB per CTA
-        const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
-        int res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
-        FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");
-        // every resident CTA holds COLS of the SM's 512 TMEM columns; a CTA
-        // beyond that would block in tcgen05.alloc, so the shared-memory
-        // request is padded until no more than 512 / COLS CTAs fit
-        const int max_res = 512 / cols;
-        if (res > max_res) {
-            const int pad_cta = smem_sm / max_res;  // (max_res + 1) * pad_cta > smem_sm
-            shm = (size_t)(pad_cta - (int)fa.sharedSizeBytes - 1024);
-            FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-            res = max_res;
-        }
-        L.shm = shm;
-        L.res = res;
-    }
-    const int res = L.res;
-    FBP_REQUIRE(res * cols <= 512, FBP_ERR_UNSUPPORTED, "forward_tc: %d CTAs/SM x %d TMEM columns > 512", res, cols);
-    if (grid <= 0) grid = res * sm_count();
-    if (pr.item_ctr) FBP_CUDA_CHECK(cudaMemsetAsync(pr.item_ctr, 0, sizeof(int32_t), st));
-    forward_pairs_tc_kernel<C><<<grid, TC_TILE, L.shm, st>>>(net, x, pr, pair_out, status);
-    FBP_LAUNCH_CHECK();
-    return FBP_OK;
+static int tc_dispatch(int mode, const fbp_net* net, const float* x, const fbp_pairs* pr, float* pair_out,
+                       int32_t* status, int grid, cudaStream_t st) {
+    if (net->ud != 1 || net->h1 != 16 || net->h2 != 16) return 1;
+    FBP_TC_TRY(2, 3 | FBP_D2_LAPLACIAN, FBP_ACT_TANH)
+    FBP_TC_TRY(2, 3, FBP_ACT_TANH)
+    FBP_TC_TRY(2, 1, FBP_ACT_TANH)
+    FBP_TC_TRY(2, 0, FBP_ACT_TANH)
+    return tc_group_act(mode, net, x, pr, pair_out, status, grid, st);
 }
-
 }  // namespace fbp
 
 extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pairs, float* pair_out,
@@ -67,17 +25,24 @@ extern "C" int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fb
                 "fbp_forward_pairs_tc: null network pointer");
     FBP_REQUIRE(pairs->sd_rec && pairs->items && pairs->n_items, FBP_ERR_INVALID,
                 "fbp_forward_pairs_tc: null pair pointer");
-    FBP_REQUIRE(net->act == FBP_ACT_TANH, FBP_ERR_UNSUPPORTED,
-                "fbp_forward_pairs_tc: only tanh networks are compiled (act=%d)", net->act);
     FBP_REQUIRE(net->ud == 1 && net->h1 == 16 && net->h2 == 16, FBP_ERR_UNSUPPORTED,
                 "fbp_forward_pairs_tc: only the xd-16-16-1 networks are compiled (got h1=%d h2=%d ud=%d)", net->h1,
                 net->h2, net->ud);
-    cudaStream_t st = fbp::as_stream(stream);
-    if (net->xd == 2 && net->d2mask == (3 | FBP_D2_LAPLACIAN))
-        return fbp::launch_forward_tc<2, 3 | FBP_D2_LAPLACIAN>(*net, x, *pairs, pair_out, status, grid, st);
-    if (net->xd == 2 && net->d2mask == 3) return fbp::launch_forward_tc<2, 3>(*net, x, *pairs, pair_out, status, grid, st);
-    if (net->xd == 2 && net->d2mask == 1) return fbp::launch_forward_tc<2, 1>(*net, x, *pairs, pair_out, status, grid, st);
-    if (net->xd == 2 && net->d2mask == 0) return fbp::launch_forward_tc<2, 0>(*net, x, *pairs, pair_out, status, grid, st);
-    fbp::set_error("fbp_forward_pairs_tc: no compiled kernel for xd=%d d2mask=%d", net->xd, net->d2mask);
+    const int r = fbp::tc_dispatch(1, net, x, pairs, pair_out, status, grid, fbp::as_stream(stream));
+    if (r != 1) return r;
+    fbp::set_error("fbp_forward_pairs_tc: no compiled kernel for xd=%d d2mask=%d act=%d", net->xd, net->d2mask,
+                   net->act);
     return FBP_ERR_UNSUPPORTED;
+}
+
+extern "C" int fbp_has_tc_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act) {
+    fbp_net net{};
+    net.xd = xd;
+    net.h1 = h1;
+    net.h2 = h2;
+    net.ud = 1;
+    net.d2mask = d2mask;
+    net.act = act;
+    fbp_pairs pr{};
+    return fbp::tc_dispatch(2, &net, nullptr, &pr, nullptr, nullptr, 0, nullptr) == FBP_OK ? 1 : 0;
 }

@@ -184,7 +184,23 @@ __device__ __forceinline__ void tc_epilogue(const SParams<C>& S, uint32_t taddr,
 #pragma unroll
         for (int c = 0; c < J; ++c) z[c] = make_float2(acc[c][k], acc[c][k + 1]);
         z[0] = add2(z[0], *reinterpret_cast<const float2*>(&S.b2[k]));
-        tanh_jet_pair<C>(z, g);
+        if constexpr (C::ACT == FBP_ACT_TANH || C::ACT == FBP_ACT_FOURIER) {
+            tanh_jet_pair<C>(z, g);  // layer 2 is a plain tanh
+        } else {
+            float zs[2][J], gs[2][J];
+#pragma unroll
+            for (int c = 0; c < J; ++c) {
+                zs[0][c] = z[c].x;
+                zs[1][c] = z[c].y;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float a, tp, tpp, tppp;
+                tanh_jet<C>(zs[h], gs[h], a, tp, tpp, tppp, act_c<C, true>(S, k + h), act_o<C, true>(S, k + h));
+            }
+#pragma unroll
+            for (int c = 0; c < J; ++c) g[c] = make_float2(gs[0][c], gs[1][c]);
+        }
         const float2 w3 = *reinterpret_cast<const float2*>(&S.W3[k]);
 #pragma unroll
         for (int c = 0; c < J; ++c) o2[c] = fma2(w3, g[c], o2[c]);
@@ -300,11 +316,23 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
 #pragma unroll
                         for (int d = 0; d < XD; ++d)
                             z = fma2(make_float2(S.W1[n * XD + d], S.W1[(n + 1) * XD + d]), dup2(xn[d]), z);
-                        const float2 a = make_float2(tanh_fast(z.x), tanh_fast(z.y));
-                        const float2 tp = fma2(make_float2(-a.x, -a.y), a, dup2(1.0f));
-                        av[0][q] = a;
-                        av[1][q] = tp;
-                        if constexpr (NA > 2) av[NA - 1][q] = mul2(mul2(dup2(-2.0f), a), tp);
+                        if constexpr (C::ACT == FBP_ACT_TANH) {
+                            const float2 a = make_float2(tanh_fast(z.x), tanh_fast(z.y));
+                            const float2 tp = fma2(make_float2(-a.x, -a.y), a, dup2(1.0f));
+                            av[0][q] = a;
+                            av[1][q] = tp;
+                            if constexpr (NA > 2) av[NA - 1][q] = mul2(mul2(dup2(-2.0f), a), tp);
+                        } else {
+                            // sigma, sigma', sigma'' of the layer-1 activation c f(o z)
+                            float a0, t0, tt0, ttt0, a1, t1, tt1, ttt1;
+                            const float c0 = act_c<C, false>(S, n), o0 = act_o<C, false>(S, n);
+                            const float c1 = act_c<C, false>(S, n + 1), o1 = act_o<C, false>(S, n + 1);
+                            C::AF1::derivs(C::AF1::stored(z.x, o0), c0, o0, a0, t0, tt0, ttt0);
+                            C::AF1::derivs(C::AF1::stored(z.y, o1), c1, o1, a1, t1, tt1, ttt1);
+                            av[0][q] = make_float2(a0, a1);
+                            av[1][q] = make_float2(t0, t1);
+                            if constexpr (NA > 2) av[NA - 1][q] = make_float2(tt0, tt1);
+                        }
                     }
                     const uint32_t off = kmajor16_off(tid, n4) >> 2;
 #pragma unroll

@@ -237,9 +237,10 @@ def t_status(ps):
     return ps.takes.status
 
 
-def tc_supported(xd, h1, h2):
-    """True where the tensor-core forward kernel is compiled (xd = 2, two 16-wide hidden layers)."""
-    return xd == 2 and h1 == 16 and h2 == 16
+def tc_supported(xd, h1, h2, d2mask=3 | _lib.D2_LAPLACIAN, act=_lib.ACT_TANH):
+    """True where the tensor-core forward kernel is compiled (xd = 2, two
+    16-wide hidden layers; the jet masks and activations of fbp_has_tc_shape)."""
+    return bool(_lib.load().fbp_has_tc_shape(xd, h1, h2, d2mask, act))
 
 
 class FBPINNEngine:
@@ -296,12 +297,14 @@ class FBPINNEngine:
         self.adaptive_items = bool(adaptive_items)
         self.sm_count = torch.cuda.get_device_properties(self.device).multi_processor_count
         # forward jets on the tensor cores (3xTF32) where that kernel is compiled:
-        # None = wherever available, True = required, False = CUDA-core FMA kernel
-        tc_ok = tc_supported(self.xd, self.h1, self.h2) and self.act == _lib.ACT_TANH
+        # None = for the plain tanh FCN wherever available (for the other
+        # activations, whose sin/cos/tanh calls dominate, the FMA kernel is as
+        # fast), True = required, False = CUDA-core FMA kernel
+        tc_ok = tc_supported(self.xd, self.h1, self.h2, self.d2mask, self.act)
         if tensor_cores and not tc_ok:
-            raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} ({activation}); "
-                                       f"compiled: 2-16-16-1 tanh")
-        self.tensor_cores = tc_ok if tensor_cores is None else bool(tensor_cores)
+            raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} ({activation}, "
+                                       f"d2mask {self.d2mask}); compiled: 2-16-16-1 networks")
+        self.tensor_cores = (tc_ok and self.act == _lib.ACT_TANH) if tensor_cores is None else bool(tensor_cores)
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
         self.m1 = torch.zeros_like(self.theta)

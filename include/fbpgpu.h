@@ -270,7 +270,8 @@ int fbp_forward_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs
 /* Same records as fbp_forward_pairs, with layer 2 of every jet component on
  * the 5th-generation tensor cores (tcgen05, TF32 operands split hi + lo, three
  * products, FP32 accumulation in tensor memory).  Compiled for xd = 2 with two
- * 16-wide hidden layers only (FBP_ERR_UNSUPPORTED otherwise).  A kernel that
+ * 16-wide hidden layers only (FBP_ERR_UNSUPPORTED otherwise; see
+ * fbp_has_tc_shape for the jet masks and activations).  A kernel that
  * times out waiting for its MMAs sets FBP_STATUS_TC_TIMEOUT in *status and
  * leaves its remaining pairs unwritten.  Same reference functions as
  * fbp_forward_pairs. */
@@ -281,6 +282,10 @@ int fbp_forward_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pa
  * mask and activation (FBP_ACT_*; ud = 1), else 0.  Lets a caller fail early
  * with a clear message. */
 int fbp_has_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act);
+
+/* 1 if fbp_forward_pairs_tc is compiled for this shape, jet mask and
+ * activation, else 0. */
+int fbp_has_tc_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act);
 
 /* POU combination per point (the two segment sums and the divide of
  * fbpinns/trainers.py:162-170, on jets by the quotient rule):

@@ -8,6 +8,7 @@ largest magnitude.
 """
 
 import ctypes as C
+import math
 
 import numpy as np
 import pytest
@@ -80,3 +81,42 @@ def test_tensor_core_forward_rejects_other_shapes(cuda):
                                   _lib.ptr(ps.pair_out), _lib.ptr(status), 0, _lib.stream_ptr())
     assert rc == -3  # FBP_ERR_UNSUPPORTED
     assert b"16-16" in lib.fbp_last_error()
+
+
+def _net_layers(act, m, seed):
+    """2-16-16-1 layers of each compiled activation (adaptive parameters and
+    SIREN scales away from the defaults; FourierFCN: 8 features)."""
+    from fbpinns_gb300.networks import fourier_feature_layer
+    gen = torch.Generator().manual_seed(seed)
+    base = random_layers([2, 16, 16, 1], m, seed)
+    if act == "fourier":
+        omega = 2 * math.pi * 0.5 * torch.randn((m, 8, 2), generator=gen, dtype=torch.float64)
+        return [fourier_feature_layer(omega)] + [(w.float(), b.float()) for w, b in base[1:]]
+    scale = math.sqrt(6.0) if act in ("sin", "adaptive_sin") else 1.0
+    nx = {"sin": 0, "adaptive_tanh": 1, "adaptive_sin": 2}[act]
+    return [tuple([(w * scale).float(), (b * scale).float()] +
+                  [(0.5 + torch.rand(b.shape, generator=gen, dtype=torch.float64)).float() for _ in range(nx)])
+            for w, b in base]
+
+
+@pytest.mark.parametrize("act,d2", [("sin", 3 | 8), ("sin", 1), ("adaptive_tanh", 3 | 8), ("adaptive_tanh", 1),
+                                    ("adaptive_sin", 3 | 8), ("adaptive_sin", 1), ("fourier", 1)])
+def test_tensor_core_forward_other_activations(cuda, act, d2):
+    """SIREN, AdaptiveFCN, AdaptiveSIREN and FourierFCN 2-16-16-1 networks on
+    the tensor cores agree with the FMA kernel's records (four-level
+    decomposition, 3000 points)."""
+    static = decomposition("multilevel")
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = _net_layers(act, m, seed=13)
+    recs = []
+    for tc in (False, True):
+        eng = FBPINNEngine(static, [2, 16, 16, 1], d2, chunk=512, tensor_cores=tc, activation=act)
+        eng.set_theta(pack_layers(layers))
+        ps = eng.points(torch.rand((3000, 2), generator=torch.Generator().manual_seed(7)))
+        ps.pair_out.fill_(float("nan"))
+        eng.forward_pairs(ps)
+        torch.cuda.synchronize()
+        ps.check_status()
+        recs.append(ps.pair_out[:ps.s].clone())
+        J = eng.J
+    _check(recs[0], recs[1], J)
