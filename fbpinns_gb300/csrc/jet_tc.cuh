@@ -4,8 +4,10 @@
 // Layer 2 of the jet, z_c[k] = sum_n W2[k][n] v_c[n] (+ b2[k] for c = 0), is
 // J small GEMMs per tile of 128 pairs (M = 128 pairs, N = 16, K = 16).  The
 // layer-1 jet components factor as v_0 = a, v_{1+d} = tp * cw[:, d] and
-// v_{1+xd+s} = tpp * c2_s (tp = 1 - a^2, tpp = -2 a tp, cw = W1 / sd, c2_s the
-// sum of cw[:, d]^2 over the dims of second-derivative slot s),
+// v_{1+xd+s} = tpp * c2_s (a, tp, tpp = the activation and its first two
+// derivatives at the neuron's pre-activation: for tanh tp = 1 - a^2,
+// tpp = -2 a tp; cw = W1 / sd, c2_s the sum of cw[:, d]^2 over the dims of
+// second-derivative slot s),
 // so the pair-dependent A operands are only a, tp and tpp, and the per-neuron
 // scale moves into B: B_c = W2 diag(f_c), f_c = 1, cw[:, d] or c2_s,
 // built once per work item.  Each thread writes its pair's rows of a, tp, tpp
@@ -13,8 +15,10 @@
 // the no-swizzle K-major layout of 8-row x 16-byte core matrices; one thread
 // issues hi*hi + hi*lo + lo*hi MMAs (3xTF32, FP32 accumulation) into TMEM
 // columns [16c, 16c+16); every thread reads back its own TMEM lane (= its
-// pair) with tcgen05.ld.  The rest of the jet (tanh rules, output layer,
+// pair) with tcgen05.ld.  The rest of the jet (activation rules, output layer,
 // unnormalisation, window) stays on the CUDA cores as in forward_pairs_kernel.
+// The tiles of a work item are software-pipelined over two TMEM buffers: the
+// MMAs of tile t run while the CUDA cores finish tile t-1.
 //
 // Waits on the MMA-completion mbarrier are bounded: on a time-out the kernel
 // records FBP_STATUS_TC_TIMEOUT in the status word, stops issuing work, waits
