@@ -68,6 +68,65 @@ def problem_setup():
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, read
+    only) every 5 ms on a background thread during the timed region, so that
+    even a region of a fraction of a second gets many samples.  Falls back to
+    ``ClockSampler`` (nvidia-smi at 200 ms) when NVML cannot be loaded."""
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index):
+        import ctypes
+        import threading
+        self.C, self.threading = ctypes, threading
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        self.index = int(vis) if vis.strip().isdigit() else index
+        self.nvml = self.handle = None
+        self.rows = []
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+                return
+            self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.nvml, self.handle = nv, h
+        except (OSError, AttributeError):
+            self.nvml = None
+        self.fallback = None if self.nvml is not None else ClockSampler(index)
+
+    def _sample(self):
+        C = self.C
+        mhz, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, 1, C.byref(mx))  # NVML_CLOCK_SM
+        while not self._stop.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, C.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.handle, C.byref(rs)) == 0:
+                self.rows.append((mhz.value, mx.value, rs.value))
+            self._stop.wait(0.005)
+
+    def start(self):
+        if self.fallback is not None:
+            return self.fallback.start()
+        self._stop = self.threading.Event()
+        self.thread = self.threading.Thread(target=self._sample, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.fallback is not None:
+            return self.fallback.stop()
+        self._stop.set()
+        self.thread.join(timeout=5)
+        rows = self.rows
+        reasons = sorted({name for _, _, r in rows for bit, name in self.REASONS.items() if r & bit})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])) if rows else None,
+                "sm_max_mhz": float(max(r[1] for r in rows)) if rows else None,
+                "reasons": reasons, "samples": len(rows), "source": "nvml, 5 ms"}
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -250,7 +309,7 @@ def run_fused(args, world, rank, local):
     pairs = int(step.ps.takes.pt_off[npts].item())
     slots = int(step.ps.takes.np_off[npts].item())
 
-    clk = ClockSampler(local)
+    clk = NvmlClockSampler(local)
     barrier(world)
     torch.cuda.synchronize()
     clk.start()
