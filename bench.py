@@ -302,7 +302,8 @@ def run_fused(args, world, rank, local):
                        schedule=args.schedule, forward_chunk=args.forward_chunk)
     eng.set_theta(theta0)
     npts = args.points
-    step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
+    step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
+                     autotune=args.autotune)
     for _ in range(max(args.warmup, 3)):
         step.step()
     torch.cuda.synchronize()
@@ -335,8 +336,10 @@ def run_fused(args, world, rank, local):
     # ---- end to end through the public step API with host buffers ----------
     e2e = None
     try:
-        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                            schedule=args.schedule, forward_chunk=args.forward_chunk)
+        # the work-item sizes of the resampled step (autotuned there)
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=eng.chunk, grid=args.grid, tensor_cores=tc,
+                            schedule=args.schedule, forward_chunk=eng.forward_chunk,
+                            adaptive_items=eng.adaptive_items)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -468,6 +471,7 @@ def run_fused(args, world, rank, local):
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
                            "parallelism": f"replicas x{world}", "chunk": step.ps.chunk, "forward_chunk": step.ps.fwd_chunk, "schedule": eng.schedule,
+                           "autotuned": getattr(eng, "tuned", None),
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
@@ -584,6 +588,8 @@ def main():
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="use --chunk/--forward-chunk instead of measuring the work-item sizes on the first batch")
     ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "per_item"],
                     help="how the jet kernels' CTAs take work items")
     ap.add_argument("--no-plain", action="store_true")

@@ -1,0 +1,53 @@
+"""Work-item autotuner of the fused step.
+
+The jet kernels walk (subdomain, run of pairs) work items; how many pairs an
+item holds trades per-item set-up (weights into shared memory, tensor-core B
+operands, the tile pipeline's fill and drain, one gradient partial) against
+load balance over the SMs.  The best sizes depend on the network, the jet and
+how the pairs spread over the subdomains, so they are measured: every
+candidate (adjoint pairs per item, forward pairs per item) builds the work
+queues for the actual points and times forward + POU/loss + adjoint with CUDA
+events; the fastest is kept on the engine.  The candidates' results are
+identical up to the FP32 summation order of the per-item gradient partials.
+"""
+
+import torch
+
+DEFAULT_CANDIDATES = tuple((a, a * k) for a in (512, 1024, 2048) for k in (1, 2, 4))
+
+
+def _pass(engine, ps):
+    engine.forward_pairs(ps)
+    engine.pou_loss(ps)
+    engine.adjoint(ps)
+
+
+def tune_work_items(engine, x, caps=None, candidates=DEFAULT_CANDIDATES, reps=3):
+    """Time the step's device work (no parameter update) for each candidate
+    (adjoint chunk, forward chunk) on points x and set the fastest on the
+    engine (``engine.chunk``, ``engine.forward_chunk``; item sizes are then
+    used as given).  Needs ``engine.set_problem`` first.  Returns a dict with
+    the choice and every candidate's time in ms."""
+    x = torch.as_tensor(x, dtype=torch.float32).to(engine.device)
+    engine.adaptive_items = False
+    timings = {}
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for adj, fwd in candidates:
+        engine.chunk, engine.forward_chunk = int(adj), int(fwd)
+        ps = engine.points(x, caps=caps)
+        _pass(engine, ps)  # warm-up: per-device kernel attributes, caches
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        for _ in range(reps):
+            _pass(engine, ps)
+        b.record()
+        torch.cuda.synchronize()
+        ps.check_status()
+        timings[(int(adj), int(fwd))] = a.elapsed_time(b) / reps
+        del ps
+    best = min(timings, key=timings.get)
+    engine.chunk, engine.forward_chunk = best
+    engine.tuned = {"chunk": best[0], "forward_chunk": best[1],
+                    "timings_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in timings.items()}}
+    return engine.tuned

@@ -103,6 +103,7 @@ class Constants(ConstantsBase):
         self.device = "cuda"
         self.chunk = 1024              # pairs per adjoint work item
         self.forward_chunk = None      # pairs per forward work item (None: 4 x chunk)
+        self.autotune = True           # measure the work-item sizes on the first batch (fused step)
         self.launch_grid = 0           # CTAs of the persistent jet kernels (0 = 4 per SM)
         self.use_graph = True          # capture the step in a CUDA graph
         self.tensor_cores = None       # forward jets on tcgen05 (3xTF32): None = where compiled, True, False

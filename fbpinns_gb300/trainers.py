@@ -158,9 +158,18 @@ class FusedStep:
     """
 
     def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
-                 headroom=1.25, pipeline=None):
+                 headroom=1.25, pipeline=None, autotune=False):
         self.eng, self.opt = engine, opt
         engine.set_problem(spec)
+        if autotune:
+            # work-item sizes measured on this step's first batch of points
+            from .autotune import tune_work_items
+            if resample is not None:
+                xt = torch.empty((resample[0], engine.xd), dtype=torch.float32, device=engine.device)
+                engine.sample(xt, int(resample[3]), 1 << 32, list(resample[1]), list(resample[2]))
+            else:
+                xt = x_probe if host_points is not None else x
+            tune_work_items(engine, xt)
         self.resample = resample
         self.host = host_points is not None
         self.use_graph = use_graph
@@ -456,7 +465,8 @@ class FBPINNTrainer:
                         step.set_state(state)
                     else:
                         step = FusedStep(eng, spec, opt, x=training_x, resample=res, use_graph=c.use_graph,
-                                         headroom=c.pair_headroom)
+                                         headroom=c.pair_headroom,
+                                         autotune=c.autotune and getattr(eng, "tuned", None) is None)
                 elif use_plain:
                     from .plain import PlainStep
                     step = PlainStep(eng, problem, all_params, required[0], opt, x=training_x, resample=res,

@@ -587,3 +587,33 @@ def test_fast_tanh_error(cuda):
     err = (y.double() - ref).abs().max().item()
     assert err < 2.5e-7, err
     assert torch.all(y.abs() <= 1.0)
+
+
+def test_work_item_autotuner(cuda):
+    """The autotuner times every candidate on the actual points, keeps the
+    fastest on the engine, and the step then uses exactly those item sizes
+    (and gives the same loss as an engine set to them by hand)."""
+    from fbpinns_gb300.autotune import tune_work_items
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=6)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    x = torch.rand((1 << 14, 2), generator=torch.Generator().manual_seed(4))
+    eng = _engine(static, layers, 3 | _lib.D2_LAPLACIAN, chunk=1024)
+    eng.set_problem(spec)
+    cands = [(256, 256), (256, 1024), (512, 2048)]
+    tuned = tune_work_items(eng, x, candidates=cands)
+    assert set(tuned["timings_ms"]) == {f"{a}/{f}" for a, f in cands}
+    best = min(cands, key=lambda c: tuned["timings_ms"][f"{c[0]}/{c[1]}"])
+    assert (eng.chunk, eng.forward_chunk) == best == (tuned["chunk"], tuned["forward_chunk"])
+    ps = eng.points(x)
+    assert (ps.chunk, ps.fwd_chunk) == best
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    ref = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=best[0], forward_chunk=best[1],
+                       adaptive_items=False)
+    ref.set_theta(eng.theta.clone())
+    ref.set_problem(spec)
+    ps2 = ref.points(x)
+    ref.forward_pairs(ps2)
+    assert ref.pou_loss(ps2).item() == loss
