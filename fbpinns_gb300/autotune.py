@@ -13,7 +13,19 @@ identical up to the FP32 summation order of the per-item gradient partials.
 
 import torch
 
-DEFAULT_CANDIDATES = tuple((a, a * k) for a in (512, 1024, 2048) for k in (1, 2, 4))
+
+def default_candidates(s, m, sms):
+    """Around the pair-count heuristic (``engine.work_item_sizes`` with the
+    requested 1024 / 4096): adjoint items of half, once and twice its size,
+    forward items of 1, 2 and 4 times the adjoint's (at most 8192)."""
+    from .engine import work_item_sizes
+    adj, _, _ = work_item_sizes(s, m, sms, 1024, 4096)
+    out = []
+    for a in (max(64, adj // 2), adj, 2 * adj):
+        for k in (1, 2, 4):
+            if (a, min(a * k, 8192)) not in out:
+                out.append((a, min(a * k, 8192)))
+    return out
 
 
 def _pass(engine, ps):
@@ -22,13 +34,18 @@ def _pass(engine, ps):
     engine.adjoint(ps)
 
 
-def tune_work_items(engine, x, caps=None, candidates=DEFAULT_CANDIDATES, reps=3):
+def tune_work_items(engine, x, caps=None, candidates=None, reps=3):
     """Time the step's device work (no parameter update) for each candidate
     (adjoint chunk, forward chunk) on points x and set the fastest on the
     engine (``engine.chunk``, ``engine.forward_chunk``; item sizes are then
     used as given).  Needs ``engine.set_problem`` first.  Returns a dict with
-    the choice and every candidate's time in ms."""
+    the choice and every candidate's time in ms.  ``candidates`` defaults to
+    ``default_candidates`` for the pair count of x."""
     x = torch.as_tensor(x, dtype=torch.float32).to(engine.device)
+    if candidates is None:
+        probe = engine.points(x)
+        candidates = default_candidates(probe.s, engine.m, engine.sm_count)
+        del probe
     engine.adaptive_items = False
     timings = {}
     ev = lambda: torch.cuda.Event(enable_timing=True)

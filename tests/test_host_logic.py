@@ -326,3 +326,11 @@ def test_fourier_network_maps_to_a_frozen_sin_layer():
     assert torch.allclose(packed, ref, rtol=0, atol=1e-6)
     with pytest.raises(NotImplementedError):
         N.engine_network(N.FourierFCN, {"omega": omega}, layers, [xd, h, h, 1])
+
+
+def test_autotune_candidates_follow_the_pair_count():
+    from fbpinns_gb300.autotune import default_candidates
+    assert default_candidates(9_368_709, 1365, 152) == [(a, a * k) for a in (512, 1024, 2048) for k in (1, 2, 4)]
+    small = default_candidates(314_672, 128, 152)
+    assert (256, 512) in small and min(a for a, _ in small) == 128
+    assert all(f <= 8192 and f >= a for a, f in default_candidates(10 ** 9, 4096, 152))
