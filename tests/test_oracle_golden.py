@@ -250,3 +250,52 @@ def test_oracle_gradient_finite_differences():
             fd = (lp - lm).item() / (2 * h)
             got = grads[li][0][0][idx].item()
             assert abs(fd - got) <= 1e-5 * max(abs(fd), 1e-3), (li, fd, got)
+
+
+@pytest.mark.parametrize("network", ["tanh", "adaptive_sin", "fourier"])
+def test_oracle_gradient_matches_finite_differences(network):
+    """The oracle's d loss / d params (torch autograd in float64, standing in
+    for jax.grad of fbpinns/trainers.py:285-293) equals float64 central
+    differences of the oracle loss, on the HO hard-BC problem (second-order
+    jets, 15 subdomains, 60 points), for W, b and the activation parameters
+    of every layer; the frozen FourierFCN features included (zero for b)."""
+    from helpers import decomposition, oracle_params, random_layers
+    static = decomposition("ho_hardbc")
+    m = static["m"]
+    gen = torch.Generator().manual_seed(5)
+    base = random_layers([1, 8, 8, 1], m, seed=3)
+    if network == "fourier":
+        om = torch.randn((m, 4, 1), generator=gen, dtype=torch.float64) * 3.0
+        layers = [(torch.cat([om, om], 1), torch.cat([torch.zeros(m, 4), torch.full((m, 4), np.pi / 2)], 1)
+                   .double())] + [(w, b) for w, b in random_layers([8, 8, 1], m, seed=4)]
+    elif network == "adaptive_sin":
+        layers = [(w * 2.0, b, 0.5 + torch.rand(b.shape, generator=gen, dtype=torch.float64),
+                   0.5 + torch.rand(b.shape, generator=gen, dtype=torch.float64)) for w, b in base]
+    else:
+        layers = base
+    P = oracle_params(static, layers, {"sd": 0.1, "mu": 4, "k": 6400})
+    P["activation"] = network
+    x = np.random.default_rng(2).uniform(0, 1, (60, 1))
+    p = static["subdomain"]["params"]
+    takes, _, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(m, dtype=int), p[0].numpy(), p[1].numpy(),
+                                                    static["subdomain"]["pou"].numpy())
+    cons, jm = [[torch.tensor(x, dtype=torch.float64)]], [OM.get_jmaps(((0, ()), (0, (0,)), (0, (0, 0))))]
+    prob = OP.HarmonicOscillator1DHardBC
+    loss, grads, _ = OM.value_and_grad(P, a_ims, f_ims, cons, [takes], jm, prob)
+
+    def loss_at(li, k, idx, h):
+        Q = dict(P)
+        Q["layers"] = [tuple(t.clone() for t in layer) for layer in P["layers"]]
+        Q["layers"][li][k][idx] += h
+        return OM.value_and_grad(Q, a_ims, f_ims, cons, [takes], jm, prob)[0].item()
+
+    rng = np.random.default_rng(8)
+    for li, layer in enumerate(P["layers"]):
+        for k, t in enumerate(layer):
+            for _ in range(2):
+                row = int(rng.integers(len(a_ims)))
+                idx = (int(a_ims[row]),) + tuple(int(rng.integers(n)) for n in t.shape[1:])
+                h = 1e-6 * max(1.0, abs(float(t[idx])))
+                fd = (loss_at(li, k, idx, h) - loss_at(li, k, idx, -h)) / (2 * h)
+                g = float(grads[li][k][(row,) + idx[1:]])
+                assert abs(fd - g) <= 1e-5 * max(abs(g), 1e-3 * abs(loss.item())), (li, k, idx, fd, g)
