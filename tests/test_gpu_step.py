@@ -2,9 +2,9 @@
 reference's golden vectors and the float64 oracle.
 
 Tolerances (FP32 kernels vs FP64 oracle), stated per check: jets and loss
-1e-5 relative to the component's max magnitude; gradients 1e-4 relative to
-each subdomain-parameter block's max magnitude (sums over ~1e3-1e4 pairs in
-FP32)."""
+1e-5 relative to the component's max magnitude; gradients 1e-5: the largest
+difference over all parameters relative to the largest gradient magnitude
+(FP32 sums over ~1e3-1e4 pairs); trainable problem parameters 1e-4."""
 
 import math
 
@@ -26,7 +26,7 @@ from fbpinns_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 JET_TOL = 1e-5
-GRAD_TOL = 1e-4
+GRAD_TOL = 1e-5
 
 
 def _engine(static, layers, d2mask, chunk=64, activation="tanh"):
@@ -132,7 +132,7 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     grad = eng.adjoint(ps).cpu().numpy()
     ps.check_status()
     assert abs(loss - loss_ref) <= JET_TOL * abs(loss_ref), (loss, loss_ref)
-    assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
+    assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, e
     inactive = np.setdiff1d(np.arange(static["m"]), a_ims)
     assert np.all(grad[inactive] == 0)
 
@@ -173,7 +173,7 @@ def test_network_fused_loss_and_gradient_vs_oracle(cuda, name, lap, act):
     grad = eng.adjoint(ps).cpu().numpy()
     ps.check_status()
     assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
-    assert rel_err(grad[a_ims], g_ref) < GRAD_TOL
+    assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, e
 
 
 @pytest.mark.parametrize("name,lap", [("ho_hardbc", False), ("poisson", False), ("poisson", True)])
@@ -212,7 +212,7 @@ def test_fourier_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     n_feat = 8 * xd + 8  # W1 and b1 of the feature layer
     assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
     assert np.all(grad[:, :n_feat] == 0)
-    assert rel_err(grad[a_ims][:, n_feat:], g_ref) < GRAD_TOL
+    assert (e := rel_err(grad[a_ims][:, n_feat:], g_ref)) < GRAD_TOL, e
 
 
 def test_laplacian_jets_match_sum_of_second_derivatives(cuda):
@@ -276,7 +276,7 @@ def test_generic_path_matches_fused(cuda):
     loss_g = pcls.loss_fn(all_params, [[xc] + ujs])
     loss_g.backward()
     assert abs(loss_g.item() - loss_f) <= 1e-5 * abs(loss_f)
-    assert rel_err(theta.grad.cpu().numpy(), grad_f.cpu().numpy()) < GRAD_TOL
+    assert (e := rel_err(theta.grad.cpu().numpy(), grad_f.cpu().numpy())) < GRAD_TOL, e
 
 
 def test_generic_two_constraints_and_inverse_vs_oracle(cuda):
@@ -319,7 +319,7 @@ def test_generic_two_constraints_and_inverse_vs_oracle(cuda):
                                             trainable_problem_keys=tuple(pt_.keys()))
         assert abs(loss.item() - lref.item()) <= 1e-5 * abs(lref.item()), (pcls.__name__, loss.item(), lref.item())
         gpack = torch.cat([t.reshape(len(a_ims), -1) for dw, db in gref for t in (dw, db)], 1).numpy()
-        assert rel_err(gtheta.cpu().numpy()[a_ims], gpack) < GRAD_TOL, pcls.__name__
+        assert (e := rel_err(gtheta.cpu().numpy()[a_ims], gpack)) < GRAD_TOL, (e, pcls.__name__)
         for k in pt_:
             assert abs(gprob[k].item() - gpr[k].item()) <= 1e-4 * max(abs(gpr[k].item()), 1e-6)
 
@@ -371,7 +371,7 @@ def test_plain_step_matches_fused(cuda):
     loss_p = pstep.loss(theta)
     (g,) = torch.autograd.grad(loss_p, [theta])
     assert abs(loss_p.item() - loss_f) <= 1e-5 * abs(loss_f)
-    assert rel_err(g.cpu().numpy(), grad_f) < GRAD_TOL
+    assert (e := rel_err(g.cpu().numpy(), grad_f)) < GRAD_TOL, e
 
 
 def test_resampled_graph_step_is_deterministic_and_matches_eager(cuda):
