@@ -417,8 +417,8 @@ def run_fused(args, world, rank, local):
     ach = (fl_adj if dom == "adjoint_pairs" else fl_fwd) / (timings[dom] * 1e-3) / 1e12
     # DRAM traffic of the adjoint per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
     # adjoint_pairs_kernel<Cfg<2,16,16,11>> in one capture of this workload at 2^16 points
-    # (52.59 MB + 0.24 MB for 2,342,187 pairs), scaled by this run's pairs (traffic grows with the pairs)
-    traffic = (52.589568e6 + 0.243968e6) / 2342187 * pairs if (dom == "adjoint_pairs" and J == 4) else None
+    # (52.60 MB + 0.50 MB for 2,342,187 pairs), scaled by this run's pairs (traffic grows with the pairs)
+    traffic = (52.6016e6 + 0.502528e6) / 2342187 * pairs if (dom == "adjoint_pairs" and J == 4) else None
     roofline = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": best, "unit": "TFLOP/s", "frac": ach / best,
                 "peak_source": "FP32 FMA probe (fbp_fma_probe) measured in this run; MEASURED_PEAKS.json has no FP32 figure",
                 "traffic": traffic,
