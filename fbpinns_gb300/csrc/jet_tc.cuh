@@ -118,6 +118,7 @@ __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
 
 constexpr int TC_TILE = 128;   // pairs per tile = MMA M = threads per CTA = TMEM lanes
 constexpr uint64_t TC_WAIT_NS = 200000000ull;  // 0.2 s: an MMA group takes microseconds
+constexpr uint64_t TC_TEST_WAIT_NS = 1000000ull;  // 1 ms, with FBP_STATUS_TC_TEST_NO_MMA
 
 template <class C>
 struct TcSmem {
@@ -253,6 +254,9 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
     tc_fence_after();
     const uint32_t tmem = T.tmem_base;
     constexpr uint32_t idesc = umma_idesc_tf32(TC_TILE, H2);
+    // test hook: no MMAs are issued, so the first wait runs out (short limit)
+    const bool test_no_mma = (*(volatile int32_t*)status & FBP_STATUS_TC_TEST_NO_MMA) != 0;
+    const uint64_t wait_ns = test_no_mma ? TC_TEST_WAIT_NS : TC_WAIT_NS;
     uint32_t phase = 0;
     bool failed = false;
     __shared__ int s_item;
@@ -356,7 +360,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
                 tc_fence_before();
                 __syncthreads();
                 tc_fence_after();
-                if (tid == 0) {
+                if (tid == 0 && !test_no_mma) {
                     const uint32_t buf = tmem + (uint32_t)((ti % NBUF) * J * 16);
 #pragma unroll
                     for (int c = 0; c < J; ++c) {
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             if (!stage) break;
             // every thread waits; the verdict is made CTA-uniform before the
             // warp-collective tcgen05.ld of the epilogue
-            failed = __syncthreads_or(!mbar_wait_bounded(mbar, phase, TC_WAIT_NS));
+            failed = __syncthreads_or(!mbar_wait_bounded(mbar, phase, wait_ns));
             if (failed) {
                 if (tid == 0) atomicOr(status, FBP_STATUS_TC_TIMEOUT);
                 break;
@@ -410,7 +414,7 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             }
         }
     }
-    if (failed) mbar_wait_bounded(mbar, phase, TC_WAIT_NS);  // let the timed-out MMAs finish
+    if (failed) mbar_wait_bounded(mbar, phase, wait_ns);  // let the timed-out MMAs finish
     tc_fence_before();
     __syncthreads();
     tc_fence_after();

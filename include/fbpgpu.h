@@ -77,6 +77,11 @@ extern "C" {
 #define FBP_STATUS_LEVEL_ORDER 8        /* a point's levels are not in ascending model order */
 #define FBP_STATUS_BAD_INDEX 16         /* an index out of range was skipped */
 #define FBP_STATUS_TC_TIMEOUT 32        /* a tensor-core kernel gave up waiting for its MMAs */
+/* Test hook of the time-out path, set by the caller in *status before
+ * fbp_forward_pairs_tc: the kernel issues no MMAs, so its waits (limited to
+ * 1 ms in this mode) run out; it sets FBP_STATUS_TC_TIMEOUT, frees its tensor
+ * memory and returns, leaving the context usable.  No other kernel reads it. */
+#define FBP_STATUS_TC_TEST_NO_MMA (1 << 30)
 
 /* Maximum compiled sizes. */
 #define FBP_MAX_XD 3

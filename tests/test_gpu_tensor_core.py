@@ -120,3 +120,33 @@ def test_tensor_core_forward_other_activations(cuda, act, d2):
         recs.append(ps.pair_out[:ps.s].clone())
         J = eng.J
     _check(recs[0], recs[1], J)
+
+
+def test_tensor_core_timeout_path_reports_and_recovers(cuda):
+    """Failure detection without a fault: with FBP_STATUS_TC_TEST_NO_MMA the
+    kernel issues no MMAs, its bounded waits (1 ms) run out, it reports
+    FBP_STATUS_TC_TIMEOUT, frees its tensor memory and returns; the context
+    stays usable and the next launch writes the same records as the FMA
+    kernel."""
+    static = decomposition("multilevel")
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = random_layers([2, 16, 16, 1], m, 5)
+    eng = FBPINNEngine(static, [2, 16, 16, 1], 3 | 8, chunk=512, tensor_cores=False)
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    ps = eng.points(torch.rand((3000, 2), generator=torch.Generator().manual_seed(2)))
+    eng.forward_pairs(ps)
+    ref = ps.pair_out[:ps.s].clone()
+    lib = _lib.load()
+    net, pr = eng.net_struct(None), ps.pairs_struct(False)
+    status = torch.full((1,), 1 << 30, dtype=torch.int32, device=ps.x.device)  # FBP_STATUS_TC_TEST_NO_MMA
+    _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
+                                        _lib.ptr(status), 0, _lib.stream_ptr()), "fbp_forward_pairs_tc")
+    torch.cuda.synchronize()
+    assert int(status.item()) & 32  # FBP_STATUS_TC_TIMEOUT
+    status.zero_()
+    ps.pair_out.fill_(float("nan"))
+    _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
+                                        _lib.ptr(status), 0, _lib.stream_ptr()), "fbp_forward_pairs_tc")
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    _check(ref, ps.pair_out[:ps.s].clone(), eng.J)
