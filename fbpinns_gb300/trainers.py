@@ -127,10 +127,10 @@ class StepGraph:
         _lib.check(_lib.load().fbp_graph_launch(self.exec, _lib.stream_ptr()), "fbp_graph_launch")
 
     def __del__(self):
-        if self.exec is not None and _lib is not None:
+        if self.exec is not None:
             try:
                 _lib.load().fbp_graph_exec_destroy(self.exec)
-            except Exception:  # interpreter shutdown
+            except Exception:  # interpreter shutdown: the driver releases it with the context
                 pass
 
 
@@ -169,7 +169,8 @@ class FusedStep:
                 engine.sample(xt, int(resample[3]), 1 << 32, list(resample[1]), list(resample[2]))
             else:
                 xt = x_probe if host_points is not None else x
-            tune_work_items(engine, xt)
+            if xt is not None:
+                tune_work_items(engine, xt)
         self.resample = resample
         self.host = host_points is not None
         self.use_graph = use_graph
