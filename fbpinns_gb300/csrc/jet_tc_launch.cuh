@@ -33,7 +33,7 @@ int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs& pr, f
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
         FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
-        const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the driver's 1 KiB per CTA
+        const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the CUDA runtime's 1 KiB reserved per CTA
         const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
         int res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
         FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");

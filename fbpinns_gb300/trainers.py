@@ -130,7 +130,7 @@ class StepGraph:
         if self.exec is not None:
             try:
                 _lib.load().fbp_graph_exec_destroy(self.exec)
-            except Exception:  # interpreter shutdown: the driver releases it with the context
+            except Exception:  # interpreter shutdown: the CUDA driver releases it with the context
                 pass
 
 
