@@ -480,22 +480,34 @@ class FBPINNJet(torch.autograd.Function):
         return grad, None, None
 
 
-def constrained_jets(cfn, all_params, x, U, xd, d2mask):
+def constrained_jets(cfn, all_params, x, U, xd, d2mask, need=None):
     """Jets of constraining_fn(all_params, x, u(x)) from the jets U of u.
 
     For each dim d the Taylor model u(x + t e_d) = U0 + t U_d + t^2/2 U_dd is
     pushed through cfn with nested forward-mode jvp in t (torch.func), which
     gives d/dx_d and d^2/dx_d^2 of the constrained solution exactly, for any
     constraining_fn; reverse mode through it is plain autograd.
+
+    A constraining_fn that returns its u argument itself (the identity of the
+    reference's soft-constraint problems) leaves the jets as they are: U is
+    returned.  ``need`` (optional jet indices) limits the work to the dims
+    whose components are needed; the other components are zero.
     """
     n = x.shape[0]
     J = U.shape[1]
     out = [None] * J
     u0 = U[:, 0:1]
     out[0] = cfn(all_params, x, u0)
+    if out[0] is u0:
+        return U
     ones = torch.ones((n, 1), dtype=x.dtype, device=x.device)
     zero = torch.zeros((n, 1), dtype=x.dtype, device=x.device)
     for d in range(xd):
+        comps = {1 + d} | ({jet_index(xd, d2mask, (d, d))} if (d2mask >> d) & 1 else set())
+        if need is not None and not (comps & set(need)):
+            for k in comps:
+                out[k] = torch.zeros_like(out[0])
+            continue
         e = torch.zeros((1, xd), dtype=x.dtype, device=x.device)
         e[0, d] = 1.0
         ud = U[:, 1 + d:2 + d]

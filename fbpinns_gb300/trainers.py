@@ -73,8 +73,10 @@ class GenericStep:
         for ic, con in enumerate(self.constraints):
             a, b = self.offsets[ic], self.offsets[ic] + self.sizes[ic]
             x = self.ps.x[a:b]
-            Uc = constrained_jets(self.problem.constraining_fn, self.all_params, x, U[a:b], self.xd, eng.d2mask)
-            ujs = [Uc[:, k:k + 1] for k in (jet_index(self.xd, eng.d2mask, ixs) for _, ixs in self.required[ic])]
+            ks = [jet_index(self.xd, eng.d2mask, ixs) for _, ixs in self.required[ic]]
+            Uc = constrained_jets(self.problem.constraining_fn, self.all_params, x, U[a:b], self.xd, eng.d2mask,
+                                  need=ks)
+            ujs = [Uc[:, k:k + 1] for k in ks]
             cons_.append(list(con) + ujs)
         return self.problem.loss_fn(self.all_params, cons_)
 

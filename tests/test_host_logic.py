@@ -334,3 +334,39 @@ def test_autotune_candidates_follow_the_pair_count():
     small = default_candidates(314_672, 128, 152)
     assert (256, 512) in small and min(a for a, _ in small) == 128
     assert all(f <= 8192 and f >= a for a, f in default_candidates(10 ** 9, 4096, 152))
+
+
+def test_constrained_jets_identity_and_needed_components():
+    """constrained_jets (the jets of constraining_fn(u) for the generic step):
+    exact against closed forms for the HO hard-constraint ansatz
+    u_c = 1 + tanh(t/sd)^2 u (value, first and second derivative, and the
+    gradient with respect to the input jets); an identity constraining_fn
+    returns the input jets themselves; ``need`` computes only the requested
+    dims (others zero) with the same values."""
+    from fbpinns_gb300.engine import constrained_jets
+    g = torch.Generator().manual_seed(1)
+    x = torch.rand((64, 1), generator=g, dtype=torch.float64)
+    U = torch.randn((64, 3), generator=g, dtype=torch.float64, requires_grad=True)
+    sp = PR.HarmonicOscillator1DHardBC.init_params(d=2, w0=80, sd=0.1)[0]
+    ap = {"static": {"problem": sp}, "trainable": {}}
+    cfn = PR.HarmonicOscillator1DHardBC.constraining_fn
+    Uc = constrained_jets(cfn, ap, x, U, 1, 1)
+    sd = 0.1
+    th = torch.tanh(x / sd)
+    s = th ** 2                                   # ansatz factor and its t-derivatives
+    s1 = 2 * th * (1 - th ** 2) / sd
+    s2 = (2 * (1 - th ** 2) ** 2 - 4 * th ** 2 * (1 - th ** 2)) / sd ** 2
+    u, u1, u2 = U[:, 0:1], U[:, 1:2], U[:, 2:3]
+    ref = torch.cat([1 + s * u, s1 * u + s * u1, s2 * u + 2 * s1 * u1 + s * u2], 1)
+    assert torch.allclose(Uc, ref, rtol=1e-12, atol=1e-12)
+    w = torch.randn((64, 3), generator=g, dtype=torch.float64)
+    ga, = torch.autograd.grad((Uc * w).sum(), U)
+    gb, = torch.autograd.grad((ref * w).sum(), U)
+    assert torch.allclose(ga, gb, rtol=1e-12, atol=1e-12)
+    # identity: the jets themselves
+    ident = lambda all_params, x_batch, u: u
+    assert constrained_jets(ident, ap, x, U, 1, 1) is U
+    # only the value needed: no derivative work, zeros in the rest
+    Uv = constrained_jets(cfn, ap, x, U, 1, 1, need=[0])
+    assert torch.equal(Uv[:, 0:1], Uc[:, 0:1]) and torch.all(Uv[:, 1:] == 0)
+    assert torch.equal(constrained_jets(cfn, ap, x, U, 1, 1, need=[0, 2]), Uc)
