@@ -370,3 +370,47 @@ def test_constrained_jets_identity_and_needed_components():
     Uv = constrained_jets(cfn, ap, x, U, 1, 1, need=[0])
     assert torch.equal(Uv[:, 0:1], Uc[:, 0:1]) and torch.all(Uv[:, 1:] == 0)
     assert torch.equal(constrained_jets(cfn, ap, x, U, 1, 1, need=[0, 2]), Uc)
+
+
+def test_integration_binding_matches_the_library_binding():
+    """The ctypes stub shown for the reference side declares
+    the same structures and argument types as the binding this package uses,
+    so the document cannot drift from the ABI."""
+    import ctypes as C
+    import re
+    from fbpinns_gb300 import _lib
+    here = os.path.dirname(os.path.abspath(__file__))
+    txt = open(os.path.join(here, "..", "INTEGRATION.md")).read()
+    code = re.search(r"```python\n(.*?)```", txt, re.S).group(1)
+
+    class _Fn:
+        pass
+
+    class _Lib:
+        def __getattr__(self, name):
+            f = _Fn()
+            object.__setattr__(self, name, f)
+            return f
+
+    real_cdll = C.CDLL
+    C.CDLL = lambda *a, **k: _Lib()
+    try:
+        ns = {}
+        exec(code, ns)
+    finally:
+        C.CDLL = real_cdll
+    for st in ("Boxes", "Net", "Pairs", "Problem"):
+        doc = [(n, t.__name__) for n, t in ns[st]._fields_]
+        ours = [(n, t.__name__) for n, t in getattr(_lib, st)._fields_]
+        assert doc == ours, st
+    lib = ns["lib"]
+    checked = 0
+    for name, (res, args) in _lib._SIG.items():
+        f = lib.__dict__.get(name)
+        if f is None or not hasattr(f, "argtypes"):
+            continue
+        norm = lambda ts: [t.__name__ if not hasattr(t, "_type_") or not isinstance(t._type_, type)
+                           else "P:" + t._type_.__name__ for t in ts]
+        assert norm(f.argtypes) == norm(args), name
+        checked += 1
+    assert checked >= 15
