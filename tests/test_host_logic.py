@@ -414,3 +414,32 @@ def test_integration_binding_matches_the_library_binding():
         assert norm(f.argtypes) == norm(args), name
         checked += 1
     assert checked >= 15
+
+
+def test_header_constants_match_the_python_binding():
+    """Activation codes, status bits, jet-mask flags and problem ids of
+    include/fbpgpu.h equal the constants the Python side passes."""
+    import re
+    from fbpinns_gb300 import _lib
+    here = os.path.dirname(os.path.abspath(__file__))
+    hdr = open(os.path.join(here, "..", "include", "fbpgpu.h")).read()
+    vals = {}
+    for name, expr in re.findall(r"^#define (FBP_[A-Z0-9_]+) ([^/\n]+)", hdr, re.M):
+        try:
+            vals[name] = eval(expr.strip(), {})
+        except Exception:
+            pass
+    assert vals["FBP_D2_LAPLACIAN"] == _lib.D2_LAPLACIAN
+    assert all(_lib.D2_GROUP(d) == ((d & 7) << 4) for d in range(8))
+    for key, code in _lib.ACTIVATIONS.items():
+        assert vals["FBP_ACT_" + key.upper()] == code, key
+    for bit in _lib.STATUS_BITS:
+        assert bit in (vals["FBP_STATUS_PAIR_OVERFLOW"], vals["FBP_STATUS_SLOT_OVERFLOW"],
+                       vals["FBP_STATUS_ITEM_OVERFLOW"], vals["FBP_STATUS_LEVEL_ORDER"],
+                       vals["FBP_STATUS_BAD_INDEX"], vals["FBP_STATUS_TC_TIMEOUT"])
+    ids = (_lib.PROBLEM_NONE, _lib.PROBLEM_HO_HARDBC, _lib.PROBLEM_BURGERS, _lib.PROBLEM_POISSON2D,
+           _lib.PROBLEM_WAVE_C, _lib.PROBLEM_HELMHOLTZ2D)
+    assert ids == tuple(vals[k] for k in ("FBP_PROBLEM_NONE", "FBP_PROBLEM_HO_HARDBC", "FBP_PROBLEM_BURGERS",
+                                           "FBP_PROBLEM_POISSON2D", "FBP_PROBLEM_WAVE_C",
+                                           "FBP_PROBLEM_HELMHOLTZ2D"))
+    assert vals["FBP_OK"] == _lib.FBP_OK == 0
