@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <mutex>
 
 #include "jet_tc.cuh"
 
@@ -18,38 +19,44 @@ int launch_forward_tc(const fbp_net& net, const float* x, const fbp_pairs& pr, f
         size_t shm;  // dynamic shared memory per CTA
     };
     static Launch launch_dev[FBP_MAX_DEVICES] = {};  // per device
+    static std::mutex launch_mu;  // the first launch per device sets both fields; others read a copy
     const int dev = current_device();
-    Launch& L = launch_dev[dev];
     constexpr int cols = TcSmem<C>::COLS;
-    if (!L.res) {
-        size_t shm = sizeof(TcSmem<C>);
-        FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)shm));
-        // CTAs that fit on one SM by shared memory, registers and threads: an
-        // upper bound on how many can be resident at once
-        cudaFuncAttributes fa;
-        FBP_CUDA_CHECK(cudaFuncGetAttributes(&fa, forward_pairs_tc_kernel<C>));
-        int smem_sm = 0, regs_sm = 0, thr_sm = 0;
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
-        FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
-        const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the CUDA runtime's 1 KiB reserved per CTA
-        const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
-        int res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
-        FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");
-        // every resident CTA holds COLS of the SM's 512 TMEM columns; a CTA
-        // beyond that would block in tcgen05.alloc, so the shared-memory
-        // request is padded until no more than 512 / COLS CTAs fit
-        const int max_res = 512 / cols;
-        if (res > max_res) {
-            const int pad_cta = smem_sm / max_res;  // (max_res + 1) * pad_cta > smem_sm
-            shm = (size_t)(pad_cta - (int)fa.sharedSizeBytes - 1024);
-            FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-            res = max_res;
+    Launch L;
+    {
+        std::lock_guard<std::mutex> lock(launch_mu);
+        Launch& cached = launch_dev[dev];
+        if (!cached.res) {
+            size_t shm = sizeof(TcSmem<C>);
+            FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)shm));
+            // CTAs that fit on one SM by shared memory, registers and threads: an
+            // upper bound on how many can be resident at once
+            cudaFuncAttributes fa;
+            FBP_CUDA_CHECK(cudaFuncGetAttributes(&fa, forward_pairs_tc_kernel<C>));
+            int smem_sm = 0, regs_sm = 0, thr_sm = 0;
+            FBP_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+            FBP_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+            FBP_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+            const int per_cta_smem = (int)(shm + fa.sharedSizeBytes) + 1024;  // + the CUDA runtime's 1 KiB reserved per CTA
+            const int per_cta_regs = ((fa.numRegs + 7) / 8 * 8) * TC_TILE;
+            int res = std::min(std::min(smem_sm / per_cta_smem, regs_sm / std::max(per_cta_regs, 1)), thr_sm / TC_TILE);
+            FBP_REQUIRE(res >= 1, FBP_ERR_UNSUPPORTED, "forward_tc: kernel does not fit on an SM");
+            // every resident CTA holds COLS of the SM's 512 TMEM columns; a CTA
+            // beyond that would block in tcgen05.alloc, so the shared-memory
+            // request is padded until no more than 512 / COLS CTAs fit
+            const int max_res = 512 / cols;
+            if (res > max_res) {
+                const int pad_cta = smem_sm / max_res;  // (max_res + 1) * pad_cta > smem_sm
+                shm = (size_t)(pad_cta - (int)fa.sharedSizeBytes - 1024);
+                FBP_CUDA_CHECK(cudaFuncSetAttribute(forward_pairs_tc_kernel<C>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+                res = max_res;
+            }
+            cached.shm = shm;
+            cached.res = res;
         }
-        L.shm = shm;
-        L.res = res;
+        L = cached;
     }
     const int res = L.res;
     FBP_REQUIRE(res * cols <= 512, FBP_ERR_UNSUPPORTED, "forward_tc: %d CTAs/SM x %d TMEM columns > 512", res, cols);
