@@ -157,6 +157,9 @@ class FusedStep:
     ``host_points`` (``pipeline=True`` opt-in) the caller passes the next
     step's points as well, ``step(x_host, x_next)``, and they are copied in
     before the step.  The results are bit-identical to the serial step.
+
+    ``autotune`` first times candidate work-item sizes on the first batch of
+    points and keeps the fastest on the engine (``autotune.tune_work_items``).
     """
 
     def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
