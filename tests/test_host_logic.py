@@ -443,3 +443,23 @@ def test_header_constants_match_the_python_binding():
                                            "FBP_PROBLEM_POISSON2D", "FBP_PROBLEM_WAVE_C",
                                            "FBP_PROBLEM_HELMHOLTZ2D"))
     assert vals["FBP_OK"] == _lib.FBP_OK == 0
+
+
+@pytest.mark.parametrize("name", ["ho", "burgers", "poisson", "wave", "helmholtz"])
+def test_configurations_set_up_on_the_host(name):
+    """Each workload configuration builds its Constants and, on the host, its
+    decomposition (subdomain count as documented), problem parameters,
+    collocation batch and the fused-loss description of its problem."""
+    from fbpinns_gb300 import configs
+    m_expected = {"ho": 15, "burgers": 128, "poisson": 1365, "wave": 900, "helmholtz": 4096}[name]
+    c = configs.CONFIGS[name](n_steps=10)
+    assert c["n_steps"] == 10 and c["network"] is N.FCN
+    dec = c.decomposition.init_params(**c.decomposition_init_kwargs)[0]
+    assert dec["m"] == m_expected
+    ps, pt = c.problem.init_params(**c.problem_init_kwargs)
+    dom = c.domain.init_params(**c.domain_init_kwargs)[0]
+    all_params = {"static": {"domain": dom, "problem": ps, "decomposition": dec}, "trainable": {"problem": pt}}
+    spec = c.problem.fused_spec(all_params)
+    assert spec is not None and "kind" in spec
+    small = configs.CONFIGS[name](n_steps=10, small=True)
+    assert np.prod(small.ns[0]) <= np.prod(c.ns[0])
