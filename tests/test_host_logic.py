@@ -463,3 +463,28 @@ def test_configurations_set_up_on_the_host(name):
     assert spec is not None and "kind" in spec
     small = configs.CONFIGS[name](n_steps=10, small=True)
     assert np.prod(small.ns[0]) <= np.prod(c.ns[0])
+
+
+def test_constants_and_model_files_round_trip(tmp_path, monkeypatch):
+    """Constants files and model pickles in the reference's layout
+    (results/summaries/<run>/constants_<run>.pickle, results/models/<run>/
+    model_XXXXXXXX.jax) load back through analysis.load_model, which picks
+    the latest model when no step is given."""
+    import pickle
+    from fbpinns_gb300 import configs
+    from fbpinns_gb300.analysis import load_model
+    monkeypatch.chdir(tmp_path)
+    c = configs.ho(n_steps=10)
+    c.run = "roundtrip"
+    c.get_outdirs()
+    c.save_constants_file()
+    for i in (5, 10):
+        model = (i, {"static": {}, "trainable": {"network": {"subdomain": {"layers": [(np.ones((15, 32, 1)),)]}}}},
+                 {"count": i}, np.ones(15, dtype=int), np.zeros((1, 3)))
+        with open(c.model_out_dir + f"model_{i:08d}.jax", "wb") as f:
+            pickle.dump(model, f)
+    c2, model = load_model("roundtrip", rootdir="results/")
+    assert model[0] == 10 and model[2]["count"] == 10
+    assert c2.run == "roundtrip" and c2.network is N.FCN and c2.n_steps == 10
+    c3, model5 = load_model("roundtrip", i=5, rootdir="results/")
+    assert model5[0] == 5
