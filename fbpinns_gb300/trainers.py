@@ -94,9 +94,9 @@ class GenericStep:
         eng = self.eng
         theta = eng.theta.detach().clone().requires_grad_(True)
         loss, gtheta, gprob = self.loss_and_grads(theta)
-        count = int(eng.count.item())
         tp = self._trainable_problem()
         if tp:
+            count = int(eng.count.item())  # the shared Adam step count (a host read only when needed)
             if not hasattr(self, "_pm"):
                 self._pm = {k: (torch.zeros_like(v), torch.zeros_like(v)) for k, v in tp.items()}
             with torch.no_grad():
