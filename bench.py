@@ -65,6 +65,28 @@ def problem_setup():
     return Poisson2D, {"static": {"problem": ps}, "trainable": {}}
 
 
+def test_points():
+    g = torch.linspace(0, 1, 100)
+    X, Y = torch.meshgrid(g, g, indexing="ij")
+    return torch.stack([X.reshape(-1), Y.reshape(-1)], 1)
+
+
+def test_l1(eng, problem, all_params, x_test, u_exact):
+    """mean |u - u_exact| of the engine's current parameters at x_test."""
+    from fbpinns_gb300.trainers import FBPINNTrainer
+    u = FBPINNTrainer.predict(eng, all_params, problem, x_test)
+    return float(torch.mean(torch.abs(u_exact.float() - u)).item())
+
+
+def test_l1_theta(eng, theta, problem, all_params, x_test, u_exact):
+    """test_l1 with parameters theta (the engine's are restored afterwards)."""
+    keep = eng.theta.clone()
+    eng.set_theta(theta)
+    l1 = test_l1(eng, problem, all_params, x_test, u_exact)
+    eng.theta.copy_(keep)
+    return l1
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -80,23 +102,28 @@ class NvmlClockSampler:
         import ctypes
         import threading
         self.C, self.threading = ctypes, threading
-        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
-        self.index = int(vis) if vis.strip().isdigit() else index
+        # NVML numbers GPUs in PCI order, CUDA fastest-first: look the GPU up by
+        # its PCI bus id (then its UUID), never by the CUDA ordinal
+        self.bus_id, self.uuid = pci_ids(index)
         self.nvml = self.handle = None
         self.rows = []
         try:
             nv = ctypes.CDLL("libnvidia-ml.so.1")
             if nv.nvmlInit_v2() != 0:
-                return
+                raise OSError("nvmlInit failed")
             h = ctypes.c_void_p()
-            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
-                return
-            self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
-                nv.nvmlDeviceGetCurrentClocksThrottleReasons
-            self.nvml, self.handle = nv, h
+            found = False
+            if self.bus_id:
+                found = nv.nvmlDeviceGetHandleByPciBusId_v2(self.bus_id.encode(), ctypes.byref(h)) == 0
+            if not found and self.uuid:
+                found = nv.nvmlDeviceGetHandleByUUID(self.uuid.encode(), ctypes.byref(h)) == 0
+            if found:
+                self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                    nv.nvmlDeviceGetCurrentClocksThrottleReasons
+                self.nvml, self.handle = nv, h
         except (OSError, AttributeError):
             self.nvml = None
-        self.fallback = None if self.nvml is not None else ClockSampler(index)
+        self.fallback = None if self.nvml is not None else ClockSampler(self.bus_id or self.uuid or index)
 
     def _sample(self):
         C = self.C
@@ -124,7 +151,22 @@ class NvmlClockSampler:
         reasons = sorted({name for _, _, r in rows for bit, name in self.REASONS.items() if r & bit})
         return {"sm_mhz": float(np.median([r[0] for r in rows])) if rows else None,
                 "sm_max_mhz": float(max(r[1] for r in rows)) if rows else None,
-                "reasons": reasons, "samples": len(rows), "source": "nvml, 5 ms"}
+                "reasons": reasons, "samples": len(rows), "source": "nvml, 5 ms", "pci_bus_id": self.bus_id}
+
+
+def pci_ids(index):
+    """(PCI bus id as NVML writes it, 'GPU-<uuid>') of CUDA device ``index``,
+    either None when torch does not report it."""
+    try:
+        pr = torch.cuda.get_device_properties(index)
+    except Exception:
+        return None, None
+    bus = None
+    if all(hasattr(pr, a) for a in ("pci_domain_id", "pci_bus_id", "pci_device_id")):
+        bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+    uid = getattr(pr, "uuid", None)
+    uid = None if uid is None else ("GPU-" + str(uid) if not str(uid).startswith("GPU-") else str(uid))
+    return bus, uid
 
 
 class ClockSampler:
@@ -133,7 +175,7 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
+        self.index = index  # a PCI bus id, a UUID or (last resort) an nvidia-smi index
         self.proc = None
         self.f = None
 
@@ -161,65 +203,41 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": "nvidia-smi, 200 ms", "gpu": str(self.index)}
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (the oracle restatement of the reference step, FP32, all threads)
+# CPU baseline: the C restatement of the reference step (oracle/cstep.c) on
+# the host cores, on the full workload (all 2^18 points, all 1365 subdomains)
 # ---------------------------------------------------------------------------
-class CPUReferenceStep:
-    """One step of the reference algorithm on the host cores: the oracle's
-    restatement (per-pair parameter gathers, nested forward-mode jets, reverse-mode
-    gradient, Adam) in FP32 torch-CPU on ``n_sample`` fresh uniform points."""
-
-    def __init__(self, static, theta_cpu, n_sample, threads):
-        from oracle import model as OM
-        from fbpinns_gb300.networks import unpack_layers
-        torch.set_num_threads(threads)
-        self.OM = OM
-        self.static, self.n_sample = static, n_sample
-        p = static["subdomain"]["params"]
-        self.layers = [(w.clone(), b.clone()) for w, b in unpack_layers(theta_cpu.clone().float(), LAYERS)]
-        self.P = {"xmins": p[0].float(), "xmaxs": p[1].float(), "flags": p[4].float(), "unnorms": p[5].float(),
-                  "pou": static["subdomain"]["pou"].float(), "layers": self.layers,
-                  "problem": {"sd": 0.1, "n_freq": 6}, "problem_trainable": {}}
-        self.mu = [torch.zeros_like(t) for wb in self.layers for t in wb]
-        self.nu = [torch.zeros_like(t) for wb in self.layers for t in wb]
-        self.jm = OM.get_jmaps(((0, (0, 0)), (0, (1, 1))))
-        self.rng = np.random.default_rng(1)
-        self.count = 0
-
-    def step(self):
-        from oracle import problems as OP
-        from oracle import takes as OT
-        OM, st, P = self.OM, self.static, self.P
-        p = st["subdomain"]["params"]
-        x = self.rng.uniform(0, 1, (self.n_sample, 2)).astype(np.float32)
-        t0 = time.perf_counter()
-        takes, all_ims, (act, a_ims, f_ims) = OT.get_inputs(x, np.ones(st["m"], dtype=int), p[0].numpy(),
-                                                           p[1].numpy(), st["subdomain"]["pou"].numpy())
-        loss, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x)]], [takes], [self.jm], OP.Poisson2D)
-        ai = torch.as_tensor(a_ims, dtype=torch.long)
-        flat = [t for gw in grads for t in gw]
-        for li, (w, b) in enumerate(P["layers"]):
-            for k, t in enumerate((w, b)):
-                idx = 2 * li + k
-                g = torch.zeros_like(t)
-                g[ai] = flat[idx].to(t.dtype)
-                th, self.mu[idx], self.nu[idx], _ = OM.adam_update(t, g, self.mu[idx], self.nu[idx], self.count, LR)
-                t.copy_(th)
-        self.count += 1
-        return time.perf_counter() - t0
+def cpu_reference_step(static, theta_cpu, threads):
+    from oracle import cstep
+    p = static["subdomain"]["params"]
+    return cstep.PoissonStep([t.numpy() for t in p], static["subdomain"]["pou"].numpy(), theta_cpu.numpy(),
+                             LAYERS[1], sd=0.1, n_freq=6, threads=threads, lr=LR)
 
 
-def cpu_baseline(static, theta_cpu, threads, n_sample=1024, budget_s=10.0):
-    """Median seconds per CPU reference step over ~budget_s of work."""
-    ref = CPUReferenceStep(static, theta_cpu, n_sample, threads)
-    ref.step()
-    times, t_end = [], time.time() + budget_s
-    while len(times) < 2 or (time.time() < t_end and len(times) < 50):
-        times.append(ref.step())
-    return float(np.median(times)), len(times)
+def cpu_steps(ref, n_points, steps, warmup, seed=1, budget_s=None):
+    """Seconds per step of ``ref`` on fresh uniform points (drawn inside the
+    timed loop, as the GPU step draws its own), after ``warmup`` steps; with
+    ``budget_s`` it stops after that many seconds (at least 3 steps).
+    Returns (seconds per step, steps timed, per-stage seconds of the last step)."""
+    rng = np.random.default_rng(seed)
+    for _ in range(warmup):
+        ref.step(rng.uniform(0, 1, (n_points, 2)).astype(np.float32))
+    t0 = time.perf_counter()
+    k = 0
+    while k < steps:
+        ref.step(rng.uniform(0, 1, (n_points, 2)).astype(np.float32))
+        k += 1
+        if budget_s is not None and k >= 3 and time.perf_counter() - t0 > budget_s:
+            break
+    return (time.perf_counter() - t0) / k, k, ref.times.copy()
+
+
+CPU_KIND = ("C restatement of the reference step (oracle/cstep.c): dense point-in-box lists, per-pair FCN jets "
+            "(u, grad u, u_xx, u_yy) with activations stored for the reverse pass, POU segment sums, hard "
+            "constraint, FP64 loss sum, reverse-mode gradient, optax Adam; FP32, pthreads")
 
 
 # ---------------------------------------------------------------------------
@@ -252,28 +270,33 @@ def barrier(world):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference step restated in C, timed on the full
+    workload (2^18 points redrawn every step, all 1365 subdomains) on every
+    host core, --warmup then --steps steps; plus a sweep of the point count."""
     if rank != 0:
         return
     static = decomposition_static()
     theta = init_theta(static["m"])
     threads = os.cpu_count() or 1
-    n_sample = 1024
-    ref = CPUReferenceStep(static, theta, n_sample, threads)
-    for _ in range(args.warmup):
-        ref.step()
-    t0 = time.perf_counter()
-    per_step = [ref.step() for _ in range(args.steps)]
-    wall = time.perf_counter() - t0
-    t_step = wall / args.steps
-    value = (n_sample / N_POINTS) / t_step  # full-workload steps/s: pairs scale linearly with points
+    ref = cpu_reference_step(static, theta, threads)
+    t_step, k, stages = cpu_steps(ref, N_POINTS, args.steps, args.warmup)
+    value = 1.0 / t_step
+    sweep = {}
+    for n in (1024, 16384, N_POINTS):
+        r2 = cpu_reference_step(static, theta, threads)
+        ts, ks, _ = cpu_steps(r2, n, 3, 1, seed=2)
+        sweep[str(n)] = {"ms_per_step": 1000.0 * ts, "steps": ks, "pairs": r2.pairs}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points)",
-            "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "sample_points": n_sample},
+            "steps": k, "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
+            "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": ref.pairs,
+                       "layers": LAYERS},
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{n_sample} of {N_POINTS} uniform points per step on the full decomposition "
-                                       f"(oracle restatement, FP32 torch-CPU); steps/s scaled by "
-                                       f"{n_sample}/{N_POINTS}; median step {1000 * float(np.median(per_step)):.1f} ms"},
+                             "sample": f"{k} full steps of the workload ({N_POINTS} points, {ref.pairs} pairs); "
+                                       + CPU_KIND,
+                             "stage_s": {"lists": stages[0], "forward": stages[1], "pou_loss": stages[2],
+                                         "reverse": stages[3], "adam": stages[4]}},
+            "sample_sweep": sweep,
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -426,8 +449,16 @@ def run_fused(args, world, rank, local):
                 "kernel_ms": {k: round(v, 4) for k, v in timings.items()},
                 "algorithmic_flops_per_launch": {"forward_pairs": fl_fwd, "adjoint_pairs": fl_adj}}
 
-    # ---- plain GPU step (torch autograd) ----
+    # ---- plain GPU step (torch autograd), then the matched test error ----
+    # Both arms start from theta0 with step count 0 and draw the same points
+    # each step (the Philox stream is keyed by the seed and the step count);
+    # after the plain arm's 2 warm-up + kp timed steps, both give their test L1
+    # on a 100 x 100 grid against the exact solution (mean |u - u_exact|, as
+    # the reference's _test, fbpinns/trainers.py:727-774).
     plain = None
+    l1_fused = None
+    x_test = test_points().to(dev)
+    u_exact = problem.exact_solution(all_params, x_test).to(dev)
     if not args.no_plain:
         try:
             eng3 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk)
@@ -444,23 +475,41 @@ def run_fused(args, world, rank, local):
                 pstep.step()
             b.record()
             torch.cuda.synchronize()
+            pstep.check()
             ms_p = max_over_ranks(a.elapsed_time(b) / kp, world)
-            plain = {"value": world * 1000.0 / ms_p, "unit": "steps/s", "ms_per_step": ms_p, "steps": kp,
-                     "fused_over_plain": ms_p / ms_max}
+            k_match = 2 + kp
+            l1_plain = test_l1(eng3, problem, all_params, x_test, u_exact)
             del pstep, eng3
+            # the fused step (the benchmarked configuration) over the same k_match steps
+            eng4 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=eng.chunk, grid=args.grid,
+                                tensor_cores=tc, schedule=args.schedule, forward_chunk=eng.forward_chunk,
+                                adaptive_items=eng.adaptive_items)
+            eng4.set_theta(theta0)
+            fstep = FusedStep(eng4, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
+            for _ in range(k_match):
+                fstep.step()
+            torch.cuda.synchronize()
+            fstep.check()
+            l1_fused = test_l1(eng4, problem, all_params, x_test, u_exact)
+            l1_0 = test_l1_theta(eng4, theta0, problem, all_params, x_test, u_exact)
+            del fstep, eng4
+            plain = {"value": world * 1000.0 / ms_p, "unit": "steps/s", "ms_per_step": ms_p, "steps": kp,
+                     "fused_over_plain": ms_p / ms_max, "test_l1": l1_plain,
+                     "matched": {"steps": k_match, "test_l1_initial": l1_0, "test_l1_fused": l1_fused,
+                                 "test_l1_plain": l1_plain, "rel_gap": abs(l1_fused - l1_plain) / l1_plain,
+                                 "test_points": "100 x 100 grid on [0,1]^2"}}
         except Exception as ex:
             plain = {"value": None, "error": repr(ex)[:300]}
         torch.cuda.empty_cache()
 
-    # ---- CPU baseline (rank 0 only) ----
+    # ---- CPU baseline (rank 0 only): full steps of the same workload, ~10 s ----
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        n_sample = 1024
-        t_cpu, nsteps = cpu_baseline(static, theta0.cpu(), threads, n_sample)
-        cpu = {"value": (n_sample / N_POINTS) / t_cpu, "unit": "steps/s", "cores": threads, "kind": "port",
-               "sample": f"{nsteps} steps of {n_sample} of {N_POINTS} uniform points on the full decomposition "
-                         f"(oracle restatement in FP32 torch-CPU); steps/s scaled by {n_sample}/{N_POINTS}"}
+        ref = cpu_reference_step(static, theta0.cpu(), threads)
+        t_cpu, nsteps, _ = cpu_steps(ref, N_POINTS, 30, 1, budget_s=10.0)
+        cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": f"{nsteps} full steps of the workload ({N_POINTS} points, {ref.pairs} pairs); " + CPU_KIND}
 
     # launches of our kernels in one step (counted from the C-ABI calls of the step body)
     per_step = (1 + 1 + 3 + 3 + 1 + 6 + 5 + 5 + 1 + 1 + 1 + 1 + 1 + 2)
@@ -477,7 +526,7 @@ def run_fused(args, world, rank, local):
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
                                  ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
                 "e2e": e2e, "gpu_launches": per_step * args.steps, "clocks": clocks, "roofline": roofline,
-                "cpu_baseline": cpu, "plain": plain, "loss_last": loss_last,
+                "cpu_baseline": cpu, "plain": plain, "test_l1": l1_fused, "loss_last": loss_last,
                 "evals_per_s": value * pairs}
         print(json.dumps(line), flush=True)
 

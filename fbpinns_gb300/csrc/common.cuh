@@ -36,6 +36,10 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 constexpr int kSM = 152;  // GB300 SM count (grid sizing hint; queried at run time too)
 
+// Elements per tile of the exclusive int32 scan (takes.cu): its scratch holds
+// one sum per tile plus the total.
+constexpr int kScanTile = 2048;
+
 // Per-device caches (kernel attributes, occupancy-sized grids) are indexed by
 // the current device, 0 .. FBP_MAX_DEVICES - 1.
 constexpr int FBP_MAX_DEVICES = 64;

@@ -6,7 +6,8 @@
 //
 // The scan's only scratch (one int32 sum per 2048-element tile, plus the
 // total) lives in a file-scope __device__ array of fixed size.  Every GPU that
-// loads this library holds that array (32 KiB) until the process exits.
+// loads this library holds that array (about 32 KiB: 8193 int32) until the
+// process exits.
 #include <mutex>
 
 #include "common.cuh"
@@ -20,15 +21,18 @@ size_t scan_scratch(int64_t n);
 
 namespace {
 
-// Tile sums for up to FBP_SCAN_NOALLOC_MAX_N elements: ceil(n / 2048) + 1 int32.
+// Tile sums for up to FBP_SCAN_NOALLOC_MAX_N elements: ceil(n / tile) + 1 int32.
 constexpr int64_t kMaxN = FBP_SCAN_NOALLOC_MAX_N;
-constexpr int64_t kSums = (kMaxN + 2047) / 2048 + 1;
+constexpr int64_t kSums = (kMaxN + fbp::kScanTile - 1) / fbp::kScanTile + 1;
 
 static __device__ __align__(256) int32_t g_scan_sums[kSums];
 
 // Device address of g_scan_sums per device ordinal.  In host code the name
 // g_scan_sums is only a host-side stand-in for the device array, so the real
-// address is looked up once per device with that device current.
+// address is looked up once per device with that device current.  A
+// cudaDeviceReset makes the cached address stale: the entry is cleared when a
+// launch through it fails, and a caller that resets a device must not call
+// this function on it again (the library's other entry points are unaffected).
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 int32_t* g_addr[kMaxDevices] = {};
@@ -64,5 +68,13 @@ extern "C" int fbp_scan_i32_noalloc(const int32_t* in, int32_t* out, int64_t n, 
     if (rc) return rc;
     // Nothing in the array has to start at zero: each call writes every tile
     // sum (and the total) before reading it.
-    return fbp::scan_launch(in, out, n, sums, fbp::as_stream(stream));
+    const int lrc = fbp::scan_launch(in, out, n, sums, fbp::as_stream(stream));
+    if (lrc != FBP_OK) {  // look the address up again on the next call
+        int dev = -1;
+        if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices) {
+            std::lock_guard<std::mutex> lock(g_mu);
+            g_addr[dev] = nullptr;
+        }
+    }
+    return lrc;
 }

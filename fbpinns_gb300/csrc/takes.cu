@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
 // Exclusive scan of int32 (3 kernels, deterministic)
 // ---------------------------------------------------------------------------
 constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_TILE = SCAN_T * SCAN_V;
+static_assert(SCAN_TILE == kScanTile, "the scan tile is shared with the allocation-free scan");
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int* smem_warp, int& total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

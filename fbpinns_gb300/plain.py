@@ -101,12 +101,17 @@ class PlainStep:
         J, xd, d2 = eng.J, eng.xd, eng.d2mask
         sd_start = ps.sd_start.long()
         counts_all = (sd_start[1:] - sd_start[:-1])
-        u_total = int(ps.takes.np_off[ps.n].item())
+        # one host read per step: the slot count, the lists' status word and
+        # each group's largest pair count (the padded batch shapes)
+        head = torch.stack([ps.takes.np_off[ps.n].long(), ps.takes.status[0].long()] +
+                           [counts_all[ids].max() for ids in self.groups]).tolist()
+        u_total, status, maxcs = head[0], head[1], head[2:]
+        if status:
+            ps.check_status()  # raises: a fixed-capacity list overflowed
         N = torch.zeros((u_total, J), dtype=torch.float32, device=eng.device)
         Wn = torch.zeros((u_total, J), dtype=torch.float32, device=eng.device)
-        for ids in self.groups:
+        for ids, maxc in zip(self.groups, maxcs):
             counts = counts_all[ids]
-            maxc = int(counts.max().item())
             if maxc == 0:
                 continue
             UW, WW, slot = self._pair_jets(theta, ids, sd_start[ids], counts, maxc)
@@ -139,3 +144,8 @@ class PlainStep:
         (g,) = torch.autograd.grad(loss, [theta])
         eng.adam(o["learning_rate"], o["b1"], o["b2"], o["eps"], o["eps_root"], grad=g.contiguous())
         return loss.detach()
+
+    def check(self):
+        """Raise if the interaction lists of this step overflowed their fixed
+        capacities (the sticky status word of the point set)."""
+        self.ps.check_status()

@@ -107,6 +107,10 @@ class GenericStep:
         eng.adam(opt["learning_rate"], opt["b1"], opt["b2"], opt["eps"], opt["eps_root"], grad=gtheta)
         return loss
 
+    def check(self):
+        """Raise if the point set's status word records an overflow."""
+        self.ps.check_status()
+
 
 class StepGraph:
     """A captured CUDA graph instantiated by the library with per-node
@@ -436,6 +440,8 @@ class FBPINNTrainer:
         lossval = None
         for i, active_ in enumerate(scheduler):
             if active_ is not None:
+                if step is not None:
+                    step.check()  # the steps since the last check ran on complete lists
                 t0 = time.time()
                 active = np.array(active_).copy()
                 # points inside models with raw state 1 (fbpinns/trainers.py:482-507)
@@ -486,6 +492,9 @@ class FBPINNTrainer:
             i1 = i + 1
             if i1 % c.summary_freq == 0:
                 lv = float(lossval.item())
+                # the status word is sticky: an overflow of a fixed-capacity list in any
+                # step since the last check raises here (this read follows the loss's sync)
+                step.check()
                 rate = c.summary_freq / max(time.time() - start1 - report_time, 1e-9)
                 self._print_summary(i1, lv, rate, start0)
                 start1, report_time = time.time(), 0.0
@@ -496,7 +505,7 @@ class FBPINNTrainer:
                 if c.save_models and i1 % c.model_save_freq == 0:
                     self._save_model(i1, self.model_tuple(i1, eng, all_params))
                 report_time += time.time() - t2
-        if isinstance(step, FusedStep):
+        if step is not None:
             torch.cuda.synchronize()
             step.check()
         all_params["trainable"]["network"] = {"subdomain": {"layers": [

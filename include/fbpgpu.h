@@ -189,12 +189,14 @@ int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n,
 
 /* fbp_scan_i32 without a scratch argument, for callers that cannot allocate
  * device memory (so cannot pass a scratch buffer): its scratch is a fixed
- * 32 KiB array inside the library, which every GPU that loads the library
- * keeps until the process exits.  n must not exceed FBP_SCAN_NOALLOC_MAX_N
- * (FBP_ERR_CAPACITY otherwise).  The first call on each device looks up that
- * array's device address, so make it before capturing a stream into a CUDA
- * graph.  All calls share the one array: calls that overlap on the GPU (for
- * example on two streams at once) race and must be serialised by the caller.
+ * array of about 32 KiB (8193 int32) inside the library, which every GPU that
+ * loads the library keeps until the process exits.  n must not exceed
+ * FBP_SCAN_NOALLOC_MAX_N (FBP_ERR_CAPACITY otherwise).  The first call on each
+ * device looks up that array's device address, so make it before capturing a
+ * stream into a CUDA graph; the address is cached per device, so do not call
+ * it on a device again after a cudaDeviceReset of that device.  All calls
+ * share the one array: calls that overlap on the GPU (for example on two
+ * streams at once) race and must be serialised by the caller.
  * No counterpart in the reference: it is an addition of this library. */
 int fbp_scan_i32_noalloc(const int32_t* in, int32_t* out, int64_t n, void* stream);
 

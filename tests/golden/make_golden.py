@@ -1,9 +1,10 @@
 """Generate golden vectors by running the reference library's own source files.
 
-Run in a container that holds the reference checkout (default
-``/root/reference``) but not JAX::
+Run where a checkout of the reference library is available (its path is
+given by ``--ref`` or the ``FBPINNS_REFERENCE`` environment variable); JAX is
+not needed::
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <path of the reference checkout>
 
 ``jaxshim`` replaces ``jax.numpy`` by numpy, so the reference functions run
 unchanged: in float32 (JAX's default mode) for the integer interaction lists
@@ -40,9 +41,12 @@ def save(name, **arrays):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("FBPINNS_REFERENCE"),
+                    help="path of the reference checkout (default: $FBPINNS_REFERENCE)")
     ap.add_argument("--out", default=HERE, help="output folder (default: next to this script)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the reference checkout with --ref or FBPINNS_REFERENCE")
     global OUT
     OUT = args.out
     jaxshim.install()
@@ -211,7 +215,7 @@ def main():
         return (dmin > margin) & (dmax > margin)
 
     def model_case(tag, decomp, sp_params, problem, pkw, layer_sizes, xb, seed, dims, network="FCN", wscale=1.0,
-                   n_features=0):
+                   n_features=0, margin=1e-2, slim=False):
         r = np.random.default_rng(seed)
         ps_prob = problem.init_params(**pkw)[0]
         m = sp_params["m"]
@@ -223,13 +227,16 @@ def main():
             layer_sizes = [2 * n_features] + list(layer_sizes)[1:]
         for fi, fo in zip(layer_sizes[:-1], layer_sizes[1:]):
             v = wscale * np.sqrt(1 / fi)
-            layer = (jnp.array(r.uniform(-v, v, (m, fo, fi))), jnp.array(r.uniform(-v, v, (m, fo))))
+            wb = [r.uniform(-v, v, (m, fo, fi)), r.uniform(-v, v, (m, fo))]
+            if slim:  # multiples of 2^-12: exact in float32, so they are stored as float32
+                wb = [np.round(t * 4096.0) / 4096.0 for t in wb]
+            layer = (jnp.array(wb[0]), jnp.array(wb[1]))
             # adaptive activations: per-neuron parameters away from their initial 1
             nx = {"AdaptiveFCN": 1, "AdaptiveSIREN": 2}.get(network, 0)
             layer += tuple(jnp.array(r.uniform(0.5, 1.5, (m, fo))) for _ in range(nx))
             layers.append(layer)
         sub = sp_params["subdomain"]["params"]
-        keep = far_from_edges(xb, np.asarray(sub[0]), np.asarray(sub[1]), 1e-2)
+        keep = far_from_edges(xb, np.asarray(sub[0]), np.asarray(sub[1]), margin)
         xb = xb[keep].astype(np.float64)
         all_params = {"static": {"decomposition": sp_params, "problem": ps_prob},
                       "trainable": {"network": {"subdomain": {"layers": layers}}}}
@@ -264,6 +271,9 @@ def main():
         # reference loss on the FD jets
         cons = problem.sample_constraints  # noqa: F841  (constraint layout documented by the problem)
         arrays["loss"] = np.float64(loss_fns[tag](all_params, xb, u, jets))
+        if slim:  # what the jet tests read: points, weights (float32-exact), POU output and its jets
+            arrays = {k: (np.asarray(v, np.float32) if k[0] in "Wb" else v) for k, v in arrays.items()
+                      if k in ("x_batch", "u_raw", "loss") or k.startswith(("raw_d", "W", "b"))}
         save(f"model_{tag}.npz", **arrays)
 
     loss_fns = {}
@@ -317,6 +327,28 @@ def main():
     loss_fns["multilevel_fourier"] = loss_fns["multilevel"]
     model_case("multilevel_fourier", DM, spm, BU, dict(), [2, 8, 1], rng_f.uniform(0, 1, (600, 2)), 22, [0, 1],
                network="FourierFCN", n_features=4)
+
+    # 2-16-16-1 networks on the full six-level decomposition (levels 1, 2, 4,
+    # 8, 16, 32 per dim, m = 1365): the benchmarked shape.  Box edges are
+    # dense at the finest level, so the points keep a 2e-3 margin from every
+    # edge (the difference stencils reach 5e-4).  Own generator: the draws
+    # above are unchanged.
+    rng_p = np.random.default_rng(41)
+    spp, _ = DM.init_params(sxs, sws, (0., 1.))
+    loss_fns["poisson16"] = loss_fns["multilevel"]
+    model_case("poisson16", DM, spp, BU, dict(), [2, 16, 16, 1], rng_p.uniform(0, 1, (2000, 2)), 24, [0, 1],
+               margin=2e-3, slim=True)
+
+    # the reference's own wave field (problems.py:408-474: the seismic CPML
+    # finite-difference solver) on a small grid, for the test of the
+    # leapfrog field that stands in for it
+    srcw = np.array([[0.1, -0.2, 0.15, 1.0], [-0.3, 0.25, 0.2, 0.5]])
+    apw2 = {"static": {"problem": WV.init_params(c0=1.0, source=srcw)[0]}}
+    bsw = (41, 41, 6)
+    xw3 = np.asarray(domains.RectangularDomainND._rectangle_samplerND(
+        None, "grid", jnp.array(np.array([-1., -1., 0.])), jnp.array(np.array([1., 1., 0.5])), bsw))
+    uw3 = WV.exact_solution(apw2, xw3, bsw)
+    save("wave_exact.npz", x=xw3, u=np.asarray(uw3), source=srcw, c0=np.float64(1.0), batch_shape=np.array(bsw))
 
     # constraining functions and losses on given jets
     xc = rng.uniform([-1, -1, 0], [1, 1, 1], (64, 3))

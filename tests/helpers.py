@@ -25,10 +25,13 @@ def decomposition(recipe):
         sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8)]
         sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
         return D.MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
-    if recipe == "poisson":
+    if recipe in ("poisson", "poisson16"):
         sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8, 16, 32)]
         sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
         return D.MultilevelRectangularDecompositionND.init_params(sxs, sws, (0., 1.))[0]
+    if recipe == "wave_full":  # the wave configuration: 15x15x4 boxes, width 2.9 x spacing
+        sx = [np.linspace(-1, 1, 15), np.linspace(-1, 1, 15), np.linspace(0, 1, 4)]
+        return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.9), (0., 1.))[0]
     if recipe in ("wave", "wave3d"):
         sx = [np.linspace(-1, 1, 5), np.linspace(-1, 1, 4), np.linspace(0, 1, 3)]
         return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.0), (0.5, 2.0))[0]
@@ -43,6 +46,13 @@ def boxes_static(xmin, xmax, pou=None):
     params = [torch.as_tensor(xmin), torch.as_tensor(xmax), z, z, torch.ones((m, 1)),
               torch.tensor([[0.0, 1.0]]).repeat(m, 1)]
     return {"m": m, "xd": xd, "subdomain": {"params": params, "pou": pou}}
+
+
+def wave_sources(seed=0, n=12, wlo=0.02):
+    """The wave configuration's initial field: n Gaussians (centres U[-0.5,
+    0.5]^2, widths U[wlo, 0.2], amplitude 1) in the (k, 4) source layout."""
+    rng = np.random.default_rng(seed)
+    return np.concatenate([rng.uniform(-0.5, 0.5, (n, 2)), rng.uniform(wlo, 0.2, (n, 1)), np.ones((n, 1))], 1)
 
 
 def golden_layers(g):

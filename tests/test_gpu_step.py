@@ -14,7 +14,7 @@ import torch
 
 from conftest import golden
 from helpers import (decomposition, golden_activation, golden_base, golden_layers, layer_sizes, oracle_params,
-                     rel_err, random_layers)
+                     rel_err, random_layers, wave_sources)
 from oracle import model as OM
 from oracle import problems as OP
 from oracle import takes as OT
@@ -29,8 +29,9 @@ JET_TOL = 1e-5
 GRAD_TOL = 1e-5
 
 
-def _engine(static, layers, d2mask, chunk=64, activation="tanh"):
-    eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk, activation=activation)
+def _engine(static, layers, d2mask, chunk=64, activation="tanh", tensor_cores=None):
+    eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk, activation=activation,
+                       tensor_cores=tensor_cores)
     eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
     return eng
 
@@ -60,6 +61,34 @@ def test_jets_vs_reference_golden(cuda, tag, dims, d2):
             assert rel_err(U[:, k:k + 1], g[f"raw_d{d}{d}"]) < JET_TOL, (d, d)
 
 
+
+@pytest.mark.parametrize("lap", [False, True])
+@pytest.mark.parametrize("tc", [True, False])
+def test_benchmarked_jets_vs_reference_golden(cuda, tc, lap):
+    """The benchmarked network shape (2-16-16-1) on the full six-level
+    decomposition (levels 1, 2, 4, 8, 16, 32 per dim, m = 1365): POU-combined
+    jets vs the reference model's values and float64 finite differences, with
+    the tensor-core and the FMA forward, per-dim second derivatives and the
+    Laplacian slot (u_xx + u_yy)."""
+    g = golden("model_poisson16.npz")
+    static = decomposition("poisson16")
+    assert static["m"] == 1365
+    layers = golden_layers(g)
+    d2 = 3 | (_lib.D2_LAPLACIAN if lap else 0)
+    eng = _engine(static, [tuple(t.double() for t in layer) for layer in layers], d2, chunk=1024, tensor_cores=tc)
+    assert eng.tensor_cores == tc
+    ps = eng.points(torch.tensor(g["x_batch"], dtype=torch.float32))
+    U = FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy()
+    ps.check_status()
+    assert rel_err(U[:, 0:1], g["u_raw"]) < JET_TOL
+    for d in range(2):
+        assert rel_err(U[:, 1 + d:2 + d], g[f"raw_d{d}"]) < JET_TOL, d
+    if lap:
+        assert rel_err(U[:, 3:4], g["raw_d00"] + g["raw_d11"]) < JET_TOL
+    else:
+        for d in range(2):
+            assert rel_err(U[:, 3 + d:4 + d], g[f"raw_d{d}{d}"]) < JET_TOL, (d, d)
+
 CASES = {
     # name: (recipe, layer sizes, problem class (product), product init kwargs, oracle class, oracle params, d2)
     "ho_hardbc": ("ho_hardbc", [1, 32, 32, 1], PR.HarmonicOscillator1DHardBC, dict(d=2, w0=80, sd=0.1),
@@ -74,6 +103,13 @@ CASES = {
              {"c0": 1.0, "source": torch.tensor([[0.1, -0.2, 0.3, 1.0], [-0.3, 0.2, 0.25, 0.5]], dtype=torch.float64)}, 7),
     "helmholtz": ("multilevel", [2, 32, 32, 1], PR.Helmholtz2D, dict(k=8 * math.pi, n_sources=4, seed=3),
                   OP.Helmholtz2D, None, 3),
+    # the benchmarked Poisson step: six-level decomposition (m = 1365), 2-16-16-1
+    "poisson_bench": ("poisson", [2, 16, 16, 1], PR.Poisson2D, dict(n_freq=6, sd=0.1),
+                      OP.Poisson2D, {"sd": 0.1, "n_freq": 6}, 3),
+    # the wave configuration: 15x15x4 boxes, 3-32-32-1, its 12 seeded sources
+    "wave_bench": ("wave_full", [3, 32, 32, 1], PR.WaveEquationConstantVelocity3D,
+                   dict(c0=1.0, source=wave_sources()), OP.WaveEquationConstantVelocity3D,
+                   {"c0": 1.0, "source": torch.tensor(wave_sources(), dtype=torch.float64)}, 7),
 }
 
 
@@ -83,7 +119,7 @@ def _points(recipe, n, seed):
         return rng.uniform(0, 1, (n, 1)).astype(np.float32)
     if recipe == "burgers":
         return np.stack([rng.uniform(-1, 1, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
-    if recipe == "wave":
+    if recipe in ("wave", "wave_full"):
         return np.stack([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
     return rng.uniform(0, 1, (n, 2)).astype(np.float32)
 
@@ -91,7 +127,8 @@ def _points(recipe, n, seed):
 def _required(name):
     return {"ho_hardbc": ((0, ()), (0, (0,)), (0, (0, 0))), "burgers": ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0))),
             "poisson": ((0, (0, 0)), (0, (1, 1))), "wave": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2))),
-            "helmholtz": ((0, ()), (0, (0, 0)), (0, (1, 1)))}[name]
+            "helmholtz": ((0, ()), (0, (0, 0)), (0, (1, 1))), "poisson_bench": ((0, (0, 0)), (0, (1, 1))),
+            "wave_bench": ((0, (0, 0)), (0, (1, 1)), (0, (2, 2)))}[name]
 
 
 def _oracle_loss_grad(name, static, layers64, x, prob_static):
@@ -124,6 +161,56 @@ def test_fused_loss_and_gradient_vs_oracle(cuda, name, lap):
     loss_ref, g_ref, a_ims, active = _oracle_loss_grad(name, static, layers32, x, prob_static)
     assert d2mask_of([_required(name)], x.shape[1]) | d2 == d2
     eng = _engine(static, layers32, d2 | (0 if not lap else _lib.D2_LAPLACIAN if d2 == 3 else _lib.D2_GROUP(3)))
+    eng.set_state(active)
+    eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+    ps = eng.points(torch.tensor(x))
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    assert abs(loss - loss_ref) <= JET_TOL * abs(loss_ref), (loss, loss_ref)
+    assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, e
+    inactive = np.setdiff1d(np.arange(static["m"]), a_ims)
+    assert np.all(grad[inactive] == 0)
+
+
+_BENCH_ORACLE = {}
+
+
+def _bench_case(name, n):
+    """Inputs and float64 oracle loss/gradient of a benchmarked-shape case
+    (computed once per (name, n): the parametrisations share them)."""
+    if (name, n) not in _BENCH_ORACLE:
+        recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+        static = decomposition(recipe)
+        layers64 = random_layers(ls, static["m"], seed=5)
+        layers32 = [(w.float().double(), b.float().double()) for w, b in layers64]
+        x = _points(recipe, n, 19)
+        prob_static = pcls.init_params(**pkw)[0]
+        _BENCH_ORACLE[(name, n)] = (static, layers32, x, prob_static,
+                                    _oracle_loss_grad(name, static, layers32, x, prob_static))
+    return _BENCH_ORACLE[(name, n)]
+
+
+@pytest.mark.parametrize("name,lap,tc,n", [("poisson_bench", True, True, 3000), ("poisson_bench", True, False, 3000),
+                                           ("poisson_bench", False, True, 3000), ("poisson_bench", False, False, 3000),
+                                           ("wave_bench", True, False, 1500), ("wave_bench", False, False, 1500)])
+def test_benchmarked_shapes_loss_and_gradient_vs_oracle(cuda, name, lap, tc, n):
+    """The kernel instantiations that the benchmark and the full-size
+    configurations run, at their real shapes, against the float64 oracle:
+    Poisson 2-16-16-1 on the six-level decomposition (m = 1365) with the
+    Laplacian slot (the benchmark's Cfg<2,16,16,11>) or per-dim slots
+    (Cfg<2,16,16,3>), tensor-core and FMA forward; the wave 3-32-32-1 on the
+    15x15x4 decomposition with its 12 sources, with the grouped u_xx + u_yy
+    slot (Cfg<3,32,32,55>) or per-dim slots (Cfg<3,32,32,7>).  The
+    benchmark's work-item sizes (1024 adjoint / 4096 forward pairs, cut for
+    the small pair count as in any run).  Loss 1e-5 relative, gradient 1e-5
+    of the largest gradient."""
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    static, layers32, x, prob_static, (loss_ref, g_ref, a_ims, active) = _bench_case(name, n)
+    d2e = d2 | (0 if not lap else _lib.D2_LAPLACIAN if d2 == 3 else _lib.D2_GROUP(3))
+    eng = _engine(static, layers32, d2e, chunk=1024, tensor_cores=tc)
+    assert eng.tensor_cores == tc and eng.forward_chunk == 4096
     eng.set_state(active)
     eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
     ps = eng.points(torch.tensor(x))

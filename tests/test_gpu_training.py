@@ -142,3 +142,22 @@ def test_fourier_network_trains_fused_and_reloads(cuda, tmp_path, monkeypatch):
     u_loaded = FBPINN_solution(c2, model[1], model[3], x)
     u_live = FBPINNTrainer.predict(tr.engine, tr.all_params, c.problem, x)
     assert torch.allclose(u_loaded, u_live, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("engine", ["fused", "plain"])
+def test_list_overflow_raises_during_training(cuda, engine):
+    """Pair and slot capacities too small for the resampled batches (0.3 x
+    the first batch) stop training at the first status check -- the first
+    summary step for the fused step, the first step for the plain one (it
+    reads its sizes every step) -- not after the last step: the kernels skip
+    what does not fit, so later steps would train on truncated lists."""
+    from fbpinns_gb300._lib import FBPLibraryError
+    c = configs.poisson(n_steps=40, small=True)
+    c.engine = engine
+    c.pair_headroom = 0.3
+    c.summary_freq, c.test_freq = 4, 40
+    tr = FBPINNTrainer(c)
+    with pytest.raises(FBPLibraryError, match="capacity"):
+        tr.train()
+    assert tr.history == []  # raised before the first summary line was recorded
+    assert int(tr.engine.count.item()) <= (4 if engine == "fused" else 0)

@@ -488,3 +488,24 @@ def test_constants_and_model_files_round_trip(tmp_path, monkeypatch):
     assert c2.run == "roundtrip" and c2.network is N.FCN and c2.n_steps == 10
     c3, model5 = load_model("roundtrip", i=5, rootdir="results/")
     assert model5[0] == 5
+
+
+def test_wave_field_matches_reference_cpml_solver():
+    """The leapfrog wave field that feeds the wave test error (wave_fd.py)
+    against the reference's own field (fbpinns/problems.py:408-474, its
+    seismic CPML finite-difference solver, run by tests/golden/make_golden.py)
+    on a 41 x 41 x 6 grid over [-1,1]^2 x [0,0.5] with two Gaussian sources:
+    relative L1 below 1.2% at every output time and the largest difference
+    below 2% of the field's peak (the leapfrog field is converged to 0.05%:
+    the rest is the reference solver's discretisation)."""
+    from fbpinns_gb300.problems import WaveEquationConstantVelocity3D as WV
+    from fbpinns_gb300.wave_fd import wave_exact
+    g = golden("wave_exact.npz")
+    ap = {"static": {"problem": WV.init_params(c0=float(g["c0"]), source=g["source"])[0]}}
+    bs = tuple(int(v) for v in g["batch_shape"])
+    u = wave_exact(ap, torch.tensor(g["x"]), bs).numpy().reshape(bs)
+    ur = g["u"].reshape(bs)
+    for k in range(bs[2]):
+        d = np.abs(u[..., k] - ur[..., k])
+        assert d.mean() < 0.012 * np.abs(ur[..., k]).mean(), k
+        assert d.max() < 0.02 * np.abs(ur).max(), k

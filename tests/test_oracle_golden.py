@@ -299,3 +299,70 @@ def test_oracle_gradient_matches_finite_differences(network):
                 fd = (loss_at(li, k, idx, h) - loss_at(li, k, idx, -h)) / (2 * h)
                 g = float(grads[li][k][(row,) + idx[1:]])
                 assert abs(fd - g) <= 1e-5 * max(abs(g), 1e-3 * abs(loss.item())), (li, k, idx, fd, g)
+
+
+@pytest.mark.parametrize("recipe,H,n", [("multilevel", 16, 1200), ("poisson", 16, 2500), ("multilevel", 8, 600),
+                                        ("multilevel", 32, 600)])
+def test_c_step_matches_oracle(recipe, H, n):
+    """The C restatement of the reference step (oracle/cstep.c; the timed CPU
+    baseline) against the float64 torch oracle on the Poisson problem: the
+    same pair count, loss within 1e-6 relative, gradients of every subdomain
+    within 2e-5 of the largest (FP32 arithmetic); Adam matches optax's update."""
+    from helpers import decomposition, oracle_params, random_layers, rel_err
+    from oracle import cstep
+    from oracle import problems as OP
+    from fbpinns_gb300.networks import pack_layers
+    static = decomposition(recipe)
+    m = static["m"]
+    layers = [(w.float().double(), b.float().double()) for w, b in random_layers([2, H, H, 1], m, seed=5)]
+    x = np.random.default_rng(3).uniform(0, 1, (n, 2)).astype(np.float32)
+    p = static["subdomain"]["params"]
+    P = oracle_params(static, layers, {"sd": 0.1, "n_freq": 6})
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(m, dtype=int), p[0].numpy(), p[1].numpy(),
+                                                          static["subdomain"]["pou"].numpy())
+    loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
+                                           [OM.get_jmaps(((0, (0, 0)), (0, (1, 1))))], OP.Poisson2D)
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
+    theta = pack_layers([tuple(t.float() for t in layer) for layer in layers]).numpy()
+    st = cstep.PoissonStep([t.numpy() for t in p], static["subdomain"]["pou"].numpy(), theta, H, threads=4)
+    loss, g = st.loss_grad(x)
+    assert st.pairs == len(takes[0])
+    assert abs(loss / loss_ref.item() - 1) < 1e-6, (loss, loss_ref.item())
+    assert (e := rel_err(g[a_ims], g_ref)) < 2e-5, e
+    inactive = np.setdiff1d(np.arange(m), a_ims)
+    assert np.all(g[inactive] == 0)
+    # one Adam step (the shared count starts at 0) against optax's update rule
+    th0 = st.theta.copy()
+    st.step(x)
+    upd = OM.adam_update(torch.tensor(th0, dtype=torch.float64), torch.tensor(st.grad, dtype=torch.float64),
+                         torch.zeros(th0.shape, dtype=torch.float64), torch.zeros(th0.shape, dtype=torch.float64),
+                         0, 1e-3)[0].numpy()
+    assert int(st.count[0]) == 1
+    assert np.abs(st.theta - upd).max() < 1e-6
+
+
+def test_six_level_model_and_jets_match_reference():
+    """The benchmarked shape: 2-16-16-1 networks on the six-level
+    decomposition (m = 1365).  The oracle's POU-combined output (before the
+    constraint) equals the reference's FBPINN_model run on numpy (1e-10), and
+    its nested-jvp jets equal float64 finite differences of it (2e-6)."""
+    from fbpinns_gb300.constants import get_subdomain_ws
+    g = golden("model_poisson16.npz")
+    sxs = [[np.array([0.5])] * 2] + [[np.linspace(0, 1, k)] * 2 for k in (2, 4, 8, 16, 32)]
+    sws = [[np.array([1.0])] * 2] + [get_subdomain_ws(s, 2.9) for s in sxs[1:]]
+    ps = OM.multilevel_params(sxs, sws, (0., 1.))
+    m = ps[0].shape[0]
+    assert m == 1365
+    x = np.asarray(g["x_batch"], dtype=np.float64)
+    takes, all_ims, _ = OT.get_inputs(x, np.ones(m, dtype=int), ps[0], ps[1], ps[6])
+    P = {"xmins": torch.tensor(ps[0]), "xmaxs": torch.tensor(ps[1]), "flags": torch.tensor(ps[4]),
+         "unnorms": torch.tensor(ps[5]), "pou": torch.tensor(ps[6]), "layers": golden_layers(g), "problem": {}}
+    P["layers"] = [tuple(t.double() for t in layer) for layer in P["layers"]]
+    P = OM.cut_params(P, all_ims)
+    req = [(0, ()), (0, (0,)), (0, (1,)), (0, (0, 0)), (0, (1, 1))]
+    ujs = OM.fbpinn_forward(P, torch.tensor(x), takes, lambda P_, xb, u: u, OM.get_jmaps(req))
+    np.testing.assert_allclose(ujs[0].numpy(), g["u_raw"], rtol=1e-10, atol=1e-12)
+    for k, nm in enumerate(["raw_d0", "raw_d1", "raw_d00", "raw_d11"]):
+        ref = g[nm]
+        err = np.abs(ujs[1 + k].numpy() - ref).max() / np.abs(ref).max()
+        assert err < 2e-6, (nm, err)
