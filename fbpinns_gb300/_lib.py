@@ -66,7 +66,7 @@ class Pairs(C.Structure):
 
 class Problem(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n_int", C.c_int32), ("p", C.c_float * 8), ("gauss", C.c_void_p),
-                ("ng", C.c_int32)]
+                ("ng", C.c_int32), ("pt_keep", C.c_void_p), ("n_keep", C.c_void_p)]
 
 
 _P = C.c_void_p
@@ -85,6 +85,8 @@ _SIG = {
     "fbp_compact_flags": (C.c_int, [_P, _I64, _P, _P, _P, C.c_size_t, _P]),
     "fbp_sort_scratch_bytes": (C.c_size_t, [_I64, _I64]),
     "fbp_sort_pairs": (C.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _P, _P, C.c_size_t, _P]),
+    "fbp_sort_pairs_kept": (C.c_int, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P, C.c_size_t, _P]),
+    "fbp_train_mask": (C.c_int, [_P, _P, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P]),
     "fbp_work_scratch_bytes": (C.c_size_t, [_I64]),
     "fbp_build_work": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, C.c_size_t, _P]),
     "fbp_forward_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _I32, _P]),

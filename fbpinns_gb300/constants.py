@@ -108,6 +108,7 @@ class Constants(ConstantsBase):
         self.use_graph = True          # capture the step in a CUDA graph
         self.tensor_cores = None       # forward jets on tcgen05 (3xTF32): None = where compiled, True, False
         self.pair_headroom = 1.25      # pair-buffer capacity factor for resampled steps
+        self.device_schedule = True    # fused step: follow scheduler changes on the device (no re-capture)
         self.save_models = False       # write model pickles at model_save_freq
         for key in kwargs:
             self[key] = kwargs[key]

@@ -536,6 +536,10 @@ __global__ void __launch_bounds__(POU_WARPS * 32) pou_loss_kernel(fbp_problem P,
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float* T = table[w];
     const float inv_npou = 1.0f / (float)npou;
+    // scheduled training: only the kept points enter the loss, whose mean is
+    // over their number (a device count written by fbp_train_mask)
+    const int32_t n_keep = P.n_keep ? max(*P.n_keep, 1) : 0;
+    if (P.n_keep) inv_n = 1.0f / (float)n_keep;
     double acc = 0.0;
     const int64_t ngroups = (n + 31) / 32;
     for (int64_t grp = (int64_t)blockIdx.x * POU_WARPS + w; grp < ngroups; grp += (int64_t)gridDim.x * POU_WARPS) {
@@ -633,7 +637,15 @@ __global__ void __launch_bounds__(POU_WARPS * 32) pou_loss_kernel(fbp_problem P,
         } else if (pv) {
             PointPOU<XD, D2>::run(p, npou, pt_off, p_take, pair_out, slot_out, u, s_cap, u_cap, status);
         }
-        if (pv) acc += (double)point_residual<XD, D2>(P, inv_n, x, p, u, U_out, ub);
+        if (pv) {
+            const float r2 = point_residual<XD, D2>(P, inv_n, x, p, u, U_out, ub);
+            if (!P.pt_keep || P.pt_keep[p]) {
+                acc += (double)r2;
+            } else {  // a point outside every active subdomain: no loss, no seeds
+#pragma unroll
+                for (int c = 0; c < J; ++c) ub[c] = 0.f;
+            }
+        }
         if (coop) {
             __syncwarp();
             if (pv) {  // seeds dL/dN_l of the point's slots, in place of U_l
@@ -668,7 +680,7 @@ __global__ void __launch_bounds__(POU_WARPS * 32) pou_loss_kernel(fbp_problem P,
         double t = 0.0;
 #pragma unroll
         for (int q = 0; q < POU_WARPS; ++q) t += sh[q];
-        loss_part[blockIdx.x] = t;
+        loss_part[blockIdx.x] = P.n_keep ? t / (double)n_keep : t;
     }
 }
 

@@ -356,7 +356,16 @@ __global__ void compact_kernel(const int32_t* __restrict__ flag, const int32_t* 
 // ---------------------------------------------------------------------------
 constexpr int SORT_CH = 4096;
 
-__global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ s_dev,
+// With pt_keep, a pair whose point has pt_keep[point] == 0 is left out (its
+// key reads as -1, outside every bucket); the kept pairs keep their order.
+__device__ __forceinline__ int kept_key(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
+                                        const uint8_t* __restrict__ pt_keep, int64_t i) {
+    const int k = key[i];
+    return (pt_keep && !pt_keep[n_take[i]]) ? -1 : k;
+}
+
+__global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
+                                 const uint8_t* __restrict__ pt_keep, const int32_t* __restrict__ s_dev,
                                  int64_t s_cap, int64_t m, int64_t nchunks, int32_t* __restrict__ hist) {
     extern __shared__ int cnt[];
     const int64_t s = min((int64_t)*s_dev, s_cap);
@@ -369,7 +378,7 @@ __global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t*
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 const int64_t i = i0 + (int64_t)u * blockDim.x + threadIdx.x;
-                kk[u] = i < b1 ? key[i] : -1;
+                kk[u] = i < b1 ? kept_key(key, n_take, pt_keep, i) : -1;
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -394,8 +403,9 @@ constexpr int SCATTER_W = 4;  // warps per chunk (fewer when 4 bucket tables do 
 // and the points of the row follow each other in order (no key matching).
 __global__ void __launch_bounds__(SCATTER_W * 32)
     sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
-                        const int32_t* __restrict__ p_take, const int32_t* __restrict__ s_dev, int64_t s_cap,
-                        int64_t m, int64_t nchunks, const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
+                        const int32_t* __restrict__ p_take, const uint8_t* __restrict__ pt_keep,
+                        const int32_t* __restrict__ s_dev, int64_t s_cap, int64_t m, int64_t nchunks,
+                        const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
     extern __shared__ int run[];  // [W][m]: per-warp counts, then running offsets
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
     int* myrun = run + (int64_t)w * m;
@@ -411,7 +421,7 @@ __global__ void __launch_bounds__(SCATTER_W * 32)
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 const int64_t i = i0 + u * 32 + lane;
-                kk[u] = i < b1 ? key[i] : -1;
+                kk[u] = i < b1 ? kept_key(key, n_take, pt_keep, i) : -1;
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -450,6 +460,7 @@ __global__ void __launch_bounds__(SCATTER_W * 32)
                     kk[u] = key[i];
                     nn[u] = n_take[i];
                     pp[u] = p_take[i];
+                    if (pt_keep && !pt_keep[nn[u]]) kk[u] = -1;
                 }
             }
 #pragma unroll
@@ -523,6 +534,42 @@ __global__ void work_fill_kernel(const int32_t* __restrict__ sd_start, int64_t m
                 *n_items = (int32_t)min((int64_t)i1, cap);
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// scheduled training: the points and subdomain states of one active mask
+// ---------------------------------------------------------------------------
+// Per point: kept when one of its boxes has raw state 1; the boxes of a kept
+// point are marked in state[] (a store of 1 by any of its points); kept
+// points are counted into *n_keep (warp sums, one atomic per warp).
+__global__ void train_mark_kernel(const int32_t* __restrict__ pt_off, const int32_t* __restrict__ m_take, int64_t n,
+                                  int64_t s_cap, const uint8_t* __restrict__ raw, uint8_t* __restrict__ pt_keep,
+                                  uint8_t* __restrict__ state, int32_t* __restrict__ n_keep) {
+    for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x; p0 < n; p0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = p0 + threadIdx.x;
+        bool keep = false;
+        if (p < n) {
+            const int64_t e0 = min((int64_t)pt_off[p], s_cap), e1 = min((int64_t)pt_off[p + 1], s_cap);
+            for (int64_t e = e0; e < e1 && !keep; ++e) keep = raw[m_take[e]] == 1;
+            pt_keep[p] = keep ? 1 : 0;
+            if (keep)
+                for (int64_t e = e0; e < e1; ++e) state[m_take[e]] = 1;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(n_keep, __popc(b));
+    }
+}
+
+// Per box: 1 (trained) where it holds a kept point and its raw state is 0 or
+// 1, 2 (fixed) where it holds one and its raw state is 2, else 0; active[j]
+// = state[j] == 1 (the adjoint's selection and Adam's mask).
+__global__ void train_state_kernel(const uint8_t* __restrict__ raw, int64_t m, uint8_t* __restrict__ state,
+                                   uint8_t* __restrict__ active) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t v = state[j] ? (raw[j] == 2 ? 2 : 1) : 0;
+        state[j] = v;
+        active[j] = v == 1 ? 1 : 0;
     }
 }
 
@@ -641,10 +688,9 @@ extern "C" size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m) {
     return (size_t)hn * sizeof(int32_t) * 2 + scan_scratch(hn) + 256;
 }
 
-extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
-                              const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_rec,
-                              void* scratch, size_t scratch_bytes,
-                              void* stream) {
+static int sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take, const uint8_t* pt_keep,
+                      const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_rec,
+                      void* scratch, size_t scratch_bytes, void* stream) {
     FBP_REQUIRE(s_dev && sd_start && m > 0, FBP_ERR_INVALID, "fbp_sort_pairs: bad args");
     FBP_REQUIRE(((uintptr_t)sd_rec & 15) == 0, FBP_ERR_INVALID, "fbp_sort_pairs: sd_rec must be 16-byte aligned");
     FBP_REQUIRE(s_cap == 0 || (m_take && n_take && p_take && sd_rec), FBP_ERR_INVALID,
@@ -669,21 +715,55 @@ extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, cons
             cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(shm * sw)));
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 8);
-        sort_hist_kernel<<<g, 256, shm, st>>>(m_take, s_dev, s_cap, m, nch, hist);
+        sort_hist_kernel<<<g, 256, shm, st>>>(m_take, n_take, pt_keep, s_dev, s_cap, m, nch, hist);
         FBP_LAUNCH_CHECK();
     }
     int rc = scan_launch(hist, hoff, hn, sums, st);
     if (rc) return rc;
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32 / sw);
-        sort_scatter_kernel<<<g, 32 * sw, shm * sw, st>>>(m_take, n_take, p_take, s_dev, s_cap, m, nch, hoff,
-                                                 reinterpret_cast<int4*>(sd_rec));
+        sort_scatter_kernel<<<g, 32 * sw, shm * sw, st>>>(m_take, n_take, p_take, pt_keep, s_dev, s_cap, m, nch,
+                                                          hoff, reinterpret_cast<int4*>(sd_rec));
         FBP_LAUNCH_CHECK();
         sort_starts_kernel<<<grid_for(m + 1, 256), 256, 0, st>>>(hoff, m, nch, sd_start);
         FBP_LAUNCH_CHECK();
     } else {
         FBP_CUDA_CHECK(cudaMemsetAsync(sd_start, 0, (size_t)(m + 1) * sizeof(int32_t), st));
     }
+    return FBP_OK;
+}
+
+extern "C" int fbp_sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
+                              const int32_t* s_dev, int64_t s_cap, int64_t m, int32_t* sd_start, int32_t* sd_rec,
+                              void* scratch, size_t scratch_bytes, void* stream) {
+    return sort_pairs(m_take, n_take, p_take, nullptr, s_dev, s_cap, m, sd_start, sd_rec, scratch, scratch_bytes,
+                      stream);
+}
+
+extern "C" int fbp_sort_pairs_kept(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
+                                   const uint8_t* pt_keep, const int32_t* s_dev, int64_t s_cap, int64_t m,
+                                   int32_t* sd_start, int32_t* sd_rec, void* scratch, size_t scratch_bytes,
+                                   void* stream) {
+    FBP_REQUIRE(pt_keep, FBP_ERR_INVALID, "fbp_sort_pairs_kept: null pt_keep");
+    return sort_pairs(m_take, n_take, p_take, pt_keep, s_dev, s_cap, m, sd_start, sd_rec, scratch, scratch_bytes,
+                      stream);
+}
+
+extern "C" int fbp_train_mask(const int32_t* pt_off, const int32_t* m_take, int64_t n, int64_t s_cap,
+                              const uint8_t* raw, int64_t m, uint8_t* pt_keep, int32_t* n_keep, uint8_t* state,
+                              uint8_t* active, void* stream) {
+    FBP_REQUIRE(pt_off && raw && pt_keep && n_keep && state && active && m > 0 && n >= 0, FBP_ERR_INVALID,
+                "fbp_train_mask: bad args");
+    FBP_REQUIRE(s_cap == 0 || m_take, FBP_ERR_INVALID, "fbp_train_mask: null m_take");
+    cudaStream_t st = as_stream(stream);
+    FBP_CUDA_CHECK(cudaMemsetAsync(state, 0, (size_t)m, st));
+    FBP_CUDA_CHECK(cudaMemsetAsync(n_keep, 0, sizeof(int32_t), st));
+    if (n > 0) {
+        train_mark_kernel<<<grid_for(n, 256), 256, 0, st>>>(pt_off, m_take, n, s_cap, raw, pt_keep, state, n_keep);
+        FBP_LAUNCH_CHECK();
+    }
+    train_state_kernel<<<grid_for(m, 256), 256, 0, st>>>(raw, m, state, active);
+    FBP_LAUNCH_CHECK();
     return FBP_OK;
 }
 

@@ -122,12 +122,19 @@ class PointSet:
     reported in ``status``.
     """
 
-    def __init__(self, engine, x, select=None, caps=None, chunk=None):
+    def __init__(self, engine, x, select=None, caps=None, chunk=None, scheduled=False):
         self.eng = engine
         g = engine.grid
         self.n = int(x.shape[0])
         self.x = x.to(g.device, torch.float32).contiguous()
         self.J = engine.J
+        # scheduled training: the training points of the engine's scheduler mask
+        # (eng.raw) are selected on the device; only their pairs are sorted into
+        # the work queues and only they enter the loss
+        self.scheduled = bool(scheduled)
+        if self.scheduled:
+            self.pt_keep = torch.zeros(max(self.n, 1), dtype=torch.uint8, device=g.device)
+            self.n_keep = torch.zeros(1, dtype=torch.int32, device=g.device)
         # requested pairs per adjoint / forward work item (the sizes used are set
         # with the buffers: smaller for small pair counts, see _allocate)
         self.chunk_req = int(chunk or engine.chunk)
@@ -187,12 +194,32 @@ class PointSet:
             if not self._sized or s > self.s_cap or u > self.u_cap:
                 self._allocate(s, u)
             self.s, self.u = s, u
+        if self.scheduled:
+            self.rebuild_scheduled(stream)
+            return
         t = self.takes
         _lib.check(lib.fbp_sort_pairs(_lib.ptr(t.m_take), _lib.ptr(t.n_take), _lib.ptr(t.p_take),
                                       _lib.ptr(t.pt_off[self.n:]), self.s_cap, eng.m, _lib.ptr(self.sd_start),
                                       _lib.ptr(self.sd_rec), _lib.ptr(self.sort_scratch), self.sort_scratch.numel() * 4, st),
                    "fbp_sort_pairs")
         self.build_work(stream, state)
+
+    def rebuild_scheduled(self, stream=None):
+        """For the lists of this point set (unchanged): the training points and
+        subdomain states of the engine's scheduler mask (eng.raw), the sort of
+        the training points' pairs and the work queues -- all on the device,
+        no host synchronisation (fbpinns/trainers.py:482-575 per mask change)."""
+        eng, t = self.eng, self.takes
+        lib = _lib.load()
+        st = _lib.stream_ptr(stream)
+        _lib.check(lib.fbp_train_mask(_lib.ptr(t.pt_off), _lib.ptr(t.m_take), self.n, self.s_cap, _lib.ptr(eng.raw),
+                                      eng.m, _lib.ptr(self.pt_keep), _lib.ptr(self.n_keep), _lib.ptr(eng.state),
+                                      _lib.ptr(eng.active), st), "fbp_train_mask")
+        _lib.check(lib.fbp_sort_pairs_kept(_lib.ptr(t.m_take), _lib.ptr(t.n_take), _lib.ptr(t.p_take),
+                                           _lib.ptr(self.pt_keep), _lib.ptr(t.pt_off[self.n:]), self.s_cap, eng.m,
+                                           _lib.ptr(self.sd_start), _lib.ptr(self.sd_rec), _lib.ptr(self.sort_scratch),
+                                           self.sort_scratch.numel() * 4, st), "fbp_sort_pairs_kept")
+        self.build_work(stream)
 
     def build_work(self, stream=None, state=None):
         """Work queues: all subdomains with pairs (forward) and the active ones (adjoint)."""
@@ -312,6 +339,9 @@ class FBPINNEngine:
         self.count = torch.zeros(1, dtype=torch.int32, device=dev)
         self.state = torch.ones(self.m, dtype=torch.uint8, device=dev)
         self.active = torch.ones(self.m, dtype=torch.uint8, device=dev)  # state == 1, the adjoint's selection
+        # the scheduler's raw mask (0 inactive, 1 active, 2 fixed) for point sets that
+        # derive state and active from it on the device (PointSet(scheduled=True))
+        self.raw = torch.ones(self.m, dtype=torch.uint8, device=dev)
         self.grad = torch.zeros_like(self.theta)
         nparts = 8 * torch.cuda.get_device_properties(dev).multi_processor_count + 1
         self.loss_part = torch.zeros(nparts, dtype=torch.float64, device=dev)
@@ -327,6 +357,14 @@ class FBPINNEngine:
         """active: (m,) ints, 0 = not trained, 1 = active, 2 = fixed (after get_inputs masking)."""
         self.state.copy_(torch.as_tensor(np.asarray(active), dtype=torch.uint8).to(self.device))
         self.active.copy_((self.state == 1).to(torch.uint8))
+
+    def set_raw_state(self, active):
+        """The scheduler's mask as it yields it (0, 1, 2 per subdomain), for
+        scheduled point sets; one host-to-device copy of m bytes."""
+        a = np.asarray(active)
+        if a.shape != (self.m,) or not np.isin(a, (0, 1, 2)).all():
+            raise ValueError(f"scheduler mask must be ({self.m},) with values 0, 1, 2")
+        self.raw.copy_(torch.as_tensor(a.astype(np.uint8)), non_blocking=False)
 
     def net_struct(self, theta=None, d2mask=None):
         g = self.grid
@@ -360,8 +398,8 @@ class FBPINNEngine:
         self._problem = pr
 
     # -- kernels -------------------------------------------------------------
-    def points(self, x, select=None, caps=None, chunk=None):
-        return PointSet(self, x, select=select, caps=caps, chunk=chunk)
+    def points(self, x, select=None, caps=None, chunk=None, scheduled=False):
+        return PointSet(self, x, select=select, caps=caps, chunk=chunk, scheduled=scheduled)
 
     def forward_pairs(self, ps, theta=None, stream=None):
         lib = _lib.load()
@@ -399,13 +437,17 @@ class FBPINNEngine:
         lib = _lib.load()
         t = ps.takes
         st = _lib.stream_ptr(stream)
+        pr = self._problem
+        pr.pt_keep, pr.n_keep = (_lib.ptr(ps.pt_keep), _lib.ptr(ps.n_keep)) if ps.scheduled else (None, None)
         _lib.check(lib.fbp_pou_loss(self.xd, self.d2mask, C.byref(self._problem), ps.n, self.npou, _lib.ptr(ps.x),
                                     _lib.ptr(t.pt_off), _lib.ptr(t.np_off), _lib.ptr(t.p_take), _lib.ptr(ps.pair_out),
                                     _lib.ptr(ps.slot_out), _lib.ptr(U_out), ps.pair_out.shape[0], ps.slot_out.shape[0],
                                     _lib.ptr(self.loss_part),
                                     self.loss_part.numel(), _lib.ptr(t.status), st), "fbp_pou_loss")
-        _lib.check(lib.fbp_loss_finalize(_lib.ptr(self.loss_part), self.loss_part.numel(), 1.0 / ps.n,
-                                         _lib.ptr(self.loss), st), "fbp_loss_finalize")
+        # a scheduled point set's partials are already divided by its training-point count
+        _lib.check(lib.fbp_loss_finalize(_lib.ptr(self.loss_part), self.loss_part.numel(),
+                                         1.0 if ps.scheduled else 1.0 / ps.n, _lib.ptr(self.loss), st),
+                   "fbp_loss_finalize")
         return self.loss
 
     def adjoint(self, ps, theta=None, out=None, stream=None, reduce=True):

@@ -167,8 +167,9 @@ class FusedStep:
     """
 
     def __init__(self, engine, spec, opt, x=None, resample=None, host_points=None, x_probe=None, use_graph=True,
-                 headroom=1.25, pipeline=None, autotune=False):
+                 headroom=1.25, pipeline=None, autotune=False, scheduled=False):
         self.eng, self.opt = engine, opt
+        self.scheduled = bool(scheduled)
         engine.set_problem(spec)
         if autotune:
             # work-item sizes measured on this step's first batch of points
@@ -197,15 +198,15 @@ class FusedStep:
             probe = engine.points(x0)
             caps = (int(probe.s * headroom) + 1024, int(probe.u * headroom) + 1024)
             del probe
-            self.ps = engine.points(x0, caps=caps)
+            self.ps = engine.points(x0, caps=caps, scheduled=self.scheduled)
         else:
-            self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(dev))
+            self.ps = engine.points(torch.as_tensor(x, dtype=torch.float32).to(dev), scheduled=self.scheduled)
         self.loss_host = torch.zeros(1, dtype=torch.float64, pin_memory=True)
         if pipeline is None:
             pipeline = resample is not None
         self.pipeline = bool(pipeline) and (resample is not None or self.host)
         if self.pipeline:
-            self.sets = [self.ps, engine.points(self.ps.x.clone(), caps=caps)]
+            self.sets = [self.ps, engine.points(self.ps.x.clone(), caps=caps, scheduled=self.scheduled)]
             self.cur = 0
             self.started = False
             self.snap = torch.zeros(1, dtype=torch.int32, device=dev)  # count at the step's start
@@ -225,8 +226,20 @@ class FusedStep:
         self.ps = ps
 
     def set_state(self, active):
+        """A new scheduler mask.  Scheduled steps take the mask as the scheduler
+        yields it (0, 1, 2): one host-to-device copy, then the training points,
+        subdomain states, pair sort and work queues are derived on the device,
+        and the captured graphs replay unchanged (their buffers are the same).
+        Other steps take the masked state (get_inputs' ``active``) and rebuild
+        their work queues."""
+        sets = self.sets if self.pipeline else [self.ps]
+        if self.scheduled:
+            self.eng.set_raw_state(active)
+            for ps in sets:
+                ps.rebuild_scheduled()
+            return
         self.eng.set_state(active)
-        for ps in (self.sets if self.pipeline else [self.ps]):
+        for ps in sets:
             ps.build_work()
         self.graph = None
         if self.pipeline:
@@ -264,6 +277,7 @@ class FusedStep:
         updates (parameters, Adam moments, step count, hence also the sampler's
         stream offset) are rolled back, so capturing does not advance training."""
         eng = self.eng
+        self.captures = getattr(self, "captures", 0) + 1
         saved = [t.clone() for t in (eng.theta, eng.m1, eng.m2, eng.count)]
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
@@ -438,8 +452,33 @@ class FBPINNTrainer:
         start0 = start1 = time.time()
         report_time = 0.0
         lossval = None
+        # Fused steps follow scheduler changes on the device: one point set over all
+        # global points, the mask copied in, the training points / states / work
+        # queues derived by kernels, the captured step replayed unchanged
+        # (resampled all-active runs keep the unmasked step: every point trains)
+        from .schedulers import AllActiveSchedulerND
+        device_sched = use_fused and getattr(c, "device_schedule", True)
+        masked = not (c.resample and c.scheduler is AllActiveSchedulerND)
         for i, active_ in enumerate(scheduler):
-            if active_ is not None:
+            if active_ is not None and device_sched:
+                if step is not None:
+                    step.check()  # the steps since the last check ran on complete lists
+                t0 = time.time()
+                active = np.array(active_).copy()
+                if step is None:
+                    res = None
+                    if c.resample:
+                        d = all_params["static"]["domain"]
+                        res = (int(np.prod(c.ns[0])), d["xmin"].tolist(), d["xmax"].tolist(), c.seed)
+                    step = FusedStep(eng, spec, opt, x=None if c.resample else x_global, resample=res,
+                                     use_graph=c.use_graph, headroom=c.pair_headroom,
+                                     autotune=c.autotune and getattr(eng, "tuned", None) is None, scheduled=masked)
+                if masked:
+                    step.set_state(active)
+                else:
+                    eng.set_state(np.where(active == 0, 1, active))
+                logger.info(f"[i: {i}/{c.n_steps}] Updating active inputs done ({time.time() - t0:.2f} s)")
+            elif active_ is not None:
                 if step is not None:
                     step.check()  # the steps since the last check ran on complete lists
                 t0 = time.time()

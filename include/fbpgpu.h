@@ -166,6 +166,12 @@ typedef struct fbp_problem {
     float p[8];           /* scalar parameters, meaning per kind (see problems.py) */
     const float* gauss;   /* (ng, 4) Gaussians [mx, my, sd, amp] (wave source, Helmholtz f) */
     int32_t ng;
+    /* Scheduled training (nullable, together): points with pt_keep[p] == 0
+     * add nothing to the loss and get no seeds, and the loss is the mean over
+     * the *n_keep kept points (both device arrays, from fbp_train_mask);
+     * fbp_loss_finalize is then called with scale 1. */
+    const uint8_t* pt_keep;
+    const int32_t* n_keep;
 } fbp_problem;
 
 /* ------------------------------------------------------------------ */
@@ -183,6 +189,28 @@ size_t fbp_scan_scratch_bytes(int64_t n);
  * fbpinns/decompositions_base.py:58). */
 int fbp_scan_i32(const int32_t* in, int32_t* out, int64_t n,
                  void* scratch, size_t scratch_bytes, void* stream);
+
+/* Scheduled training on the device: the points and subdomain states of one
+ * scheduler mask, without a host round trip.  raw (m, uint8) holds the
+ * scheduler's states (0 inactive, 1 active, 2 fixed).  For the interaction
+ * lists (pt_off, m_take) of all n points: pt_keep[p] = 1 where point p lies in
+ * a box whose raw state is 1 (the training points), *n_keep = their number;
+ * state[j] = 1 where box j holds a kept point and its raw state is 0 or 1,
+ * 2 where it holds one and is fixed, else 0; active[j] = (state[j] == 1).
+ * Replaces _get_x_batch (fbpinns/trainers.py:482-507) and the active-mask
+ * update of get_inputs (fbpinns/trainers.py:339-357). */
+int fbp_train_mask(const int32_t* pt_off, const int32_t* m_take, int64_t n, int64_t s_cap,
+                   const uint8_t* raw, int64_t m, uint8_t* pt_keep, int32_t* n_keep,
+                   uint8_t* state, uint8_t* active, void* stream);
+
+/* fbp_sort_pairs over the pairs of kept points only (pt_keep[point] != 0,
+ * from fbp_train_mask): the pairs of x_batch, the training points of the
+ * scheduler mask, in the same stable order.  Replaces the per-change
+ * re-index of the takes (fbpinns/trainers.py:509-575). */
+int fbp_sort_pairs_kept(const int32_t* m_take, const int32_t* n_take, const int32_t* p_take,
+                        const uint8_t* pt_keep, const int32_t* s_dev, int64_t s_cap, int64_t m,
+                        int32_t* sd_start, int32_t* sd_rec, void* scratch, size_t scratch_bytes,
+                        void* stream);
 
 /* Largest n accepted by fbp_scan_i32_noalloc. */
 #define FBP_SCAN_NOALLOC_MAX_N (1 << 24)

@@ -704,3 +704,45 @@ def test_work_item_autotuner(cuda):
     ps2 = ref.points(x)
     ref.forward_pairs(ps2)
     assert ref.pou_loss(ps2).item() == loss
+
+
+def test_scheduled_point_set_vs_oracle(cuda):
+    """A scheduler mask applied on the device (fbp_train_mask, the kept-pair
+    sort and the masked loss) over all global points, against the reference's
+    own _get_update_inputs for that mask (golden inputs_burgers_sched: a line
+    scheduler's mask on a 40 x 20 grid): the same subdomain states and
+    training points (bit-exact), and the loss and gradients of the oracle on
+    those training points (1e-5)."""
+    g = golden("inputs_burgers_sched.npz")
+    static = decomposition("burgers")
+    m = static["m"]
+    raw = np.asarray(g["active_in"]).astype(int)
+    x_global = np.asarray(g["x_global"], dtype=np.float32)
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES["burgers"]
+    layers32 = [(w.float().double(), b.float().double()) for w, b in random_layers(ls, m, seed=11)]
+    eng = _engine(static, layers32, d2, chunk=256)
+    prob_static = pcls.init_params(**pkw)[0]
+    eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+    eng.set_raw_state(raw)
+    ps = eng.points(torch.tensor(x_global), scheduled=True)
+    assert np.array_equal(eng.state.cpu().numpy(), np.asarray(g["active_out"]))
+    keep = ps.pt_keep[:ps.n].cpu().numpy().astype(bool)
+    assert np.array_equal(x_global[keep], np.asarray(g["x_batch"], dtype=np.float32))
+    assert int(ps.n_keep.item()) == keep.sum()
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    # oracle on the reference's training points for this mask
+    xb = x_global[keep]
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(xb, raw, p[0].numpy(), p[1].numpy(),
+                                                          static["subdomain"]["pou"].numpy())
+    assert np.array_equal(np.asarray(active), eng.state.cpu().numpy())
+    P = oracle_params(static, layers32, opar)
+    loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(xb, dtype=torch.float64)]], [takes],
+                                           [OM.get_jmaps(_required("burgers"))], ocls)
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
+    assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
+    assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, e
+    assert np.all(grad[np.setdiff1d(np.arange(m), a_ims)] == 0)

@@ -161,3 +161,38 @@ def test_list_overflow_raises_during_training(cuda, engine):
         tr.train()
     assert tr.history == []  # raised before the first summary line was recorded
     assert int(tr.engine.count.item()) <= (4 if engine == "fused" else 0)
+
+
+def test_scheduler_changes_replay_one_capture(cuda):
+    """Burgers with the line scheduler (many mask changes): the fused step
+    follows every change on the device -- one host-to-device copy of the
+    mask, the training points, states and work queues rebuilt by kernels --
+    with one graph capture in total, and gives the same losses and test
+    error as the host path that builds a new point set (and capture) per
+    change."""
+    from fbpinns_gb300.trainers import FusedStep
+    res = {}
+    for dev_sched in (True, False):
+        c = configs.burgers(n_steps=400, small=True)
+        c.summary_freq, c.test_freq = 20, 400
+        c.device_schedule = dev_sched
+        c.autotune = False
+        captures = []
+        orig = FusedStep.capture
+
+        def counted(self, *a, **k):
+            captures.append(1)
+            return orig(self, *a, **k)
+        FusedStep.capture = counted
+        try:
+            tr = FBPINNTrainer(c)
+            tr.train()
+        finally:
+            FusedStep.capture = orig
+        res[dev_sched] = ([h["loss"] for h in tr.history], tr.u_test_losses[-1][1], len(captures))
+    (l_dev, t_dev, n_dev), (l_host, t_host, n_host) = res[True], res[False]
+    assert n_dev == 1 and n_host > 1, (n_dev, n_host)
+    assert len(l_dev) == len(l_host) == 20
+    for a, b in zip(l_dev, l_host):
+        assert abs(a - b) <= 1e-4 * abs(b), (a, b)
+    assert abs(t_dev - t_host) <= 1e-4 * t_host
