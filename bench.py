@@ -321,8 +321,9 @@ def run_fused(args, world, rank, local):
     tc = False if args.fma_forward else None
     # the Poisson residual needs only the Laplacian: jets (u, u_x, u_y, u_xx + u_yy)
     d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
+    tca = args.tc_adjoint
     eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                       schedule=args.schedule, forward_chunk=args.forward_chunk)
+                       schedule=args.schedule, forward_chunk=args.forward_chunk, tc_adjoint=tca)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
@@ -360,16 +361,19 @@ def run_fused(args, world, rank, local):
     e2e = None
     try:
         # the work-item sizes of the resampled step (autotuned there)
-        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=eng.chunk, grid=args.grid, tensor_cores=tc,
-                            schedule=args.schedule, forward_chunk=eng.forward_chunk,
-                            adaptive_items=eng.adaptive_items)
+        eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
+                            tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
+                            tc_adjoint=tca)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
         host = [torch.from_numpy(rng.uniform(0, 1, (N_POINTS, 2)).astype(np.float32)).pin_memory() for _ in range(nh)]
         # pipelined: each call copies the next step's points in and builds their lists on a
         # second stream while the step trains on the current ones
-        hstep = FusedStep(eng2, spec, opt, host_points=N_POINTS, x_probe=host[0], use_graph=True, pipeline=True)
+        # the same configuration as the timed step: its tuned launch comes from the cache
+        hstep = FusedStep(eng2, spec, opt, host_points=N_POINTS, x_probe=host[0], use_graph=True, pipeline=True,
+                          autotune=args.autotune)
+        e2e_tuned = getattr(eng2, "tuned", None)
         for k in range(max(args.warmup, 3)):
             hstep.step(host[k % nh], host[(k + 1) % nh])
         torch.cuda.synchronize()
@@ -387,7 +391,7 @@ def run_fused(args, world, rank, local):
         ms_e = max_over_ranks(ms_e, world)
         hstep.check()
         e2e = {"value": world * 1000.0 / ms_e, "unit": "steps/s", "h2d_bytes_per_step": N_POINTS * 2 * 4,
-               "d2h_bytes_per_step": 8}
+               "d2h_bytes_per_step": 8, "autotune_cache": e2e_tuned and e2e_tuned.get("cache")}
         del hstep, eng2
     except Exception as ex:  # reported, not hidden
         e2e = {"value": None, "unit": "steps/s", "error": repr(ex)[:200]}
@@ -417,6 +421,11 @@ def run_fused(args, world, rank, local):
         eng.tensor_cores = True
     timed("pou_loss", lambda: eng.pou_loss(ps))
     timed("adjoint_pairs", lambda: eng.adjoint(ps, reduce=False))
+    if lib.fbp_has_tc_adjoint_shape(2, LAYERS[1], LAYERS[2], d2, _lib.ACT_TANH):
+        # the other adjoint variant on the same pairs, for comparison
+        eng.tc_adjoint = not eng.tc_adjoint
+        timed("adjoint_pairs_tc" if eng.tc_adjoint else "adjoint_pairs_fma", lambda: eng.adjoint(ps, reduce=False))
+        eng.tc_adjoint = not eng.tc_adjoint
     timed("grad_reduce", lambda: eng.reduce_grad(ps))
     timed("adam", lambda: eng.adam(0.0))
     sig = float(sum(a * b for a, b in zip(LAYERS[:-1], LAYERS[1:])))
@@ -481,11 +490,12 @@ def run_fused(args, world, rank, local):
             l1_plain = test_l1(eng3, problem, all_params, x_test, u_exact)
             del pstep, eng3
             # the fused step (the benchmarked configuration) over the same k_match steps
-            eng4 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=eng.chunk, grid=args.grid,
-                                tensor_cores=tc, schedule=args.schedule, forward_chunk=eng.forward_chunk,
-                                adaptive_items=eng.adaptive_items)
+            eng4 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
+                                tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
+                                tc_adjoint=tca)
             eng4.set_theta(theta0)
-            fstep = FusedStep(eng4, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True)
+            fstep = FusedStep(eng4, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
+                              autotune=args.autotune)
             for _ in range(k_match):
                 fstep.step()
             torch.cuda.synchronize()
@@ -519,9 +529,13 @@ def run_fused(args, world, rank, local):
                 "vs_baseline": None, "dtype": "fp32", "data": "synthetic (uniform points redrawn each step)",
                 "config": {"workload": WORKLOAD, "m": static["m"], "n_points": N_POINTS, "pairs_per_step": pairs,
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
-                           "parallelism": f"replicas x{world}", "chunk": step.ps.chunk, "forward_chunk": step.ps.fwd_chunk, "schedule": eng.schedule,
+                           "parallelism": f"replicas x{world}", "chunk": step.ps.chunk,
+                           "forward_chunk": step.ps.fwd_chunk, "schedule": eng.schedule,
+                           "grid": eng.launch_grid, "forward_grid": eng.forward_grid,
                            "autotuned": getattr(eng, "tuned", None),
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
+                           "adjoint_kernel": "tcgen05 3xTF32 layer-2 recompute + fp32 fma" if eng.tc_adjoint
+                           else "fp32 fma",
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
                                  ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
@@ -635,6 +649,8 @@ def main():
     ap.add_argument("--forward-chunk", type=int, default=0, help="pairs per forward work item (0: 4 x --chunk)")
     ap.add_argument("--grid", type=int, default=0)
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
+    ap.add_argument("--tc-adjoint", action="store_true",
+                    help="adjoint with the layer-2 recompute on the tensor cores (fbp_adjoint_pairs_tc)")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

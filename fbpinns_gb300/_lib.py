@@ -97,6 +97,8 @@ _SIG = {
                                _P, _I32, _P, _P]),
     "fbp_loss_finalize": (C.c_int, [_P, _I32, C.c_double, _P, _P]),
     "fbp_adjoint_pairs": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _P, _I32, _P]),
+    "fbp_adjoint_pairs_tc": (C.c_int, [C.POINTER(Net), _P, C.POINTER(Pairs), _P, _P, _P, _I32, _P]),
+    "fbp_has_tc_adjoint_shape": (C.c_int, [_I32, _I32, _I32, _I32, _I32]),
     "fbp_grad_reduce": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "fbp_adam": (C.c_int, [_P, _P, _P, _P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                            _P, _P]),

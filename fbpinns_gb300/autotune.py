@@ -1,17 +1,76 @@
-"""Work-item autotuner of the fused step.
+"""Launch autotuner of the fused step.
 
-The jet kernels walk (subdomain, run of pairs) work items; how many pairs an
-item holds trades per-item set-up (weights into shared memory, tensor-core B
-operands, the tile pipeline's fill and drain, one gradient partial) against
-load balance over the SMs.  The best sizes depend on the network, the jet and
-how the pairs spread over the subdomains, so they are measured: every
-candidate (adjoint pairs per item, forward pairs per item) builds the work
-queues for the actual points and times forward + POU/loss + adjoint with CUDA
-events; the fastest is kept on the engine.  The candidates' results are
-identical up to the FP32 summation order of the per-item gradient partials.
+The jet kernels walk (subdomain, run of pairs) work items.  Four launch
+choices trade against each other and depend on the network, the jet and how
+the pairs spread over the subdomains, so they are measured on the actual
+points rather than guessed:
+
+* the work-item sizes (adjoint pairs per item, forward pairs per item): per-item
+  set-up (weights into shared memory, tensor-core B operands, the tile
+  pipeline's fill and drain, one gradient partial) against load balance;
+* the schedule: ``dynamic`` (a resident grid whose CTAs take the next item from
+  a device counter), ``static`` (CTA b takes items b, b + grid, ...) or
+  ``per_item`` (one CTA per item);
+* the CTA count of the adjoint and of the forward launch (0 = every CTA that
+  can be resident, else a multiple of the SM count).
+
+The search is coordinate-wise: the item sizes first (dynamic schedule,
+resident grids), then the schedule, then the two CTA counts; every candidate
+builds the work queues for the points and times forward + POU/loss + adjoint
+with CUDA events.  The choice is kept on the engine and cached on disk, keyed
+by the GPU, the network, the jet, the subdomain count and the point and pair
+counts, so that a later run of the same configuration skips the search.  The
+candidates' results are identical up to the FP32 summation order of the
+per-item gradient partials.
 """
 
+import json
+import os
+import tempfile
+
 import torch
+
+CACHE_ENV = "FBPINNS_GB300_AUTOTUNE_CACHE"
+
+
+def cache_path():
+    """JSON file of tuned launches: $FBPINNS_GB300_AUTOTUNE_CACHE, else
+    ~/.cache/fbpinns_gb300/autotune.json."""
+    p = os.environ.get(CACHE_ENV)
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "fbpinns_gb300", "autotune.json")
+
+
+def config_key(engine, n, s):
+    """The configuration a tuned launch is valid for (pair count to 3
+    significant digits: a redrawn batch of the same size keeps the key)."""
+    s3 = float(f"{float(s):.3g}")
+    props = torch.cuda.get_device_properties(engine.device)
+    return "|".join(str(v) for v in (props.name, props.multi_processor_count, engine.layer_sizes, engine.activation,
+                                     engine.d2mask, int(engine.tensor_cores), engine.m, int(n), s3))
+
+
+def _load_cache(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(path, key, entry):
+    """Adds one entry (atomic replace: readers never see a partial file)."""
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        data = _load_cache(path)
+        data[key] = entry
+        fd, tmp = tempfile.mkstemp(dir=os.path.dirname(path), prefix=".autotune.")
+        with os.fdopen(fd, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass  # a read-only home: the choice still holds for this run
 
 
 def default_candidates(s, m, sms):
@@ -28,29 +87,52 @@ def default_candidates(s, m, sms):
     return out
 
 
+def _apply(engine, choice):
+    engine.chunk, engine.forward_chunk = int(choice["chunk"]), int(choice["forward_chunk"])
+    engine.schedule = choice["schedule"]
+    engine.launch_grid = int(choice["grid"])
+    engine.forward_grid = int(choice["forward_grid"])
+    engine.adaptive_items = False
+
+
 def _pass(engine, ps):
     engine.forward_pairs(ps)
     engine.pou_loss(ps)
     engine.adjoint(ps)
 
 
-def tune_work_items(engine, x, caps=None, candidates=None, reps=3):
-    """Time the step's device work (no parameter update) for each candidate
-    (adjoint chunk, forward chunk) on points x and set the fastest on the
-    engine (``engine.chunk``, ``engine.forward_chunk``; item sizes are then
-    used as given).  Needs ``engine.set_problem`` first.  Returns a dict with
-    the choice and every candidate's time in ms.  ``candidates`` defaults to
-    ``default_candidates`` for the pair count of x."""
+def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=True):
+    """Tune the launches of the step's device work on points x and set the
+    choice on the engine (``chunk``, ``forward_chunk``, ``schedule``,
+    ``launch_grid``, ``forward_grid``).  Needs ``engine.set_problem`` first.
+    Returns (and keeps as ``engine.tuned``) the choice, what was searched,
+    every candidate's time in ms and whether the cache held the answer."""
     x = torch.as_tensor(x, dtype=torch.float32).to(engine.device)
+    probe = engine.points(x)
+    s, n = probe.s, probe.n
     if candidates is None:
-        probe = engine.points(x)
-        candidates = default_candidates(probe.s, engine.m, engine.sm_count)
-        del probe
-    engine.adaptive_items = False
+        candidates = default_candidates(s, engine.m, engine.sm_count)
+    del probe
+    key = config_key(engine, n, s)
+    path = cache_path()
+    if use_cache:
+        hit = _load_cache(path).get(key)
+        if hit is not None:
+            _apply(engine, hit["choice"])
+            engine.tuned = dict(hit, cache="hit", key=key)
+            return engine.tuned
+    sms = engine.sm_count
+    searched = {"item_sizes": [f"{a}/{f}" for a, f in candidates], "schedule": ["dynamic", "static", "per_item"],
+                "grid": [0, sms, 2 * sms, 3 * sms], "forward_grid": [0, sms, 2 * sms]}
     timings = {}
     ev = lambda: torch.cuda.Event(enable_timing=True)
-    for adj, fwd in candidates:
-        engine.chunk, engine.forward_chunk = int(adj), int(fwd)
+
+    def run(choice):
+        tag = f"{choice['chunk']}/{choice['forward_chunk']} {choice['schedule']} g{choice['grid']} " \
+              f"fg{choice['forward_grid']}"
+        if tag in timings:
+            return timings[tag]
+        _apply(engine, choice)
         ps = engine.points(x, caps=caps)
         _pass(engine, ps)  # warm-up: per-device kernel attributes, caches
         torch.cuda.synchronize()
@@ -61,10 +143,29 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3):
         b.record()
         torch.cuda.synchronize()
         ps.check_status()
-        timings[(int(adj), int(fwd))] = a.elapsed_time(b) / reps
         del ps
-    best = min(timings, key=timings.get)
-    engine.chunk, engine.forward_chunk = best
-    engine.tuned = {"chunk": best[0], "forward_chunk": best[1],
-                    "timings_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in timings.items()}}
+        timings[tag] = a.elapsed_time(b) / reps
+        return timings[tag]
+
+    best = {"chunk": candidates[0][0], "forward_chunk": candidates[0][1], "schedule": "dynamic", "grid": 0,
+            "forward_grid": 0}
+    best_t = None
+    stages = [("size", [dict(chunk=a, forward_chunk=f) for a, f in candidates]),
+              ("schedule", [dict(schedule=v) for v in searched["schedule"]]),
+              ("grid", [dict(grid=v) for v in searched["grid"]]),
+              ("forward_grid", [dict(forward_grid=v) for v in searched["forward_grid"]])]
+    for name, opts in stages:
+        if name in ("grid", "forward_grid") and best["schedule"] == "per_item":
+            continue  # one CTA per item: the grid is the item count
+        for o in opts:
+            c = dict(best, **o)
+            t = run(c)
+            if best_t is None or t < best_t:
+                best, best_t = c, t
+    _apply(engine, best)
+    entry = {"choice": best, "searched": searched, "best_ms": round(best_t, 4),
+             "timings_ms": {k: round(v, 4) for k, v in timings.items()}}
+    if use_cache:
+        _store_cache(path, key, entry)
+    engine.tuned = dict(entry, cache="miss", key=key)
     return engine.tuned

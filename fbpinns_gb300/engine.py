@@ -274,7 +274,7 @@ class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
-                 activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True):
+                 activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True, tc_adjoint=None):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -311,6 +311,9 @@ class FBPINNEngine:
         # operands, the tile pipeline's fill and drain) is larger
         self.forward_chunk = int(forward_chunk) if forward_chunk else 4 * self.chunk
         self.launch_grid = int(grid) if grid else 0
+        # CTAs of the forward launch when set (0 = every CTA that can be
+        # resident); None: the same as launch_grid.  Set by the autotuner.
+        self.forward_grid = None
         # how the jet kernels' CTAs take work items (the results do not depend on it):
         #   "dynamic"   a resident grid; each CTA takes the next item from a device counter
         #   "static"    a resident grid; CTA b takes items b, b + grid, ...
@@ -332,6 +335,13 @@ class FBPINNEngine:
             raise _lib.FBPLibraryError(f"no tensor-core forward kernel for layer sizes {ls} ({activation}, "
                                        f"d2mask {self.d2mask}); compiled: 2-16-16-1 networks")
         self.tensor_cores = (tc_ok and self.act == _lib.ACT_TANH) if tensor_cores is None else bool(tensor_cores)
+        # adjoint with the layer-2 recompute on the tensor cores (fbp_adjoint_pairs_tc):
+        # None = off unless requested; True = required; False = off
+        tca_ok = bool(_lib.load().fbp_has_tc_adjoint_shape(self.xd, self.h1, self.h2, self.d2mask, self.act))
+        if tc_adjoint and not tca_ok:
+            raise _lib.FBPLibraryError(f"no tensor-core adjoint kernel for layer sizes {ls} ({activation}, "
+                                       f"d2mask {self.d2mask}); compiled: xd-16-16-1 tanh networks")
+        self.tc_adjoint = bool(tc_adjoint) and tca_ok
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
         self.m1 = torch.zeros_like(self.theta)
@@ -405,7 +415,8 @@ class FBPINNEngine:
         lib = _lib.load()
         net = self.net_struct(theta)
         pr = ps.pairs_struct(False)
-        grid = ps.forward_items_cap if self.schedule == "per_item" else self.launch_grid
+        grid = ps.forward_items_cap if self.schedule == "per_item" else \
+            (self.launch_grid if self.forward_grid is None else self.forward_grid)
         if self.tensor_cores:
             _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),
                                                 _lib.ptr(ps.takes.status), grid, _lib.stream_ptr(stream)),
@@ -456,8 +467,13 @@ class FBPINNEngine:
         net = self.net_struct(theta)
         pr = ps.pairs_struct(True)
         grid = ps.items_cap if self.schedule == "per_item" else self.launch_grid
-        _lib.check(lib.fbp_adjoint_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
-                                         _lib.ptr(ps.grad_part), grid, st), "fbp_adjoint_pairs")
+        if self.tc_adjoint:
+            _lib.check(lib.fbp_adjoint_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
+                                                _lib.ptr(ps.grad_part), _lib.ptr(ps.takes.status), grid, st),
+                       "fbp_adjoint_pairs_tc")
+        else:
+            _lib.check(lib.fbp_adjoint_pairs(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
+                                             _lib.ptr(ps.grad_part), grid, st), "fbp_adjoint_pairs")
         if not reduce:
             return None
         return self.reduce_grad(ps, out, stream)

@@ -365,6 +365,21 @@ int fbp_loss_finalize(const double* loss_part, int32_t n_part, double scale,
 int fbp_adjoint_pairs(const fbp_net* net, const float* x, const fbp_pairs* pairs,
                       const float* slot_out, float* grad_part, int32_t grid, void* stream);
 
+/* fbp_adjoint_pairs with the layer-2 recompute on the tensor cores: per tile
+ * of 128 pairs the jets z_c = W2 v_c of the forward are J tcgen05 GEMMs
+ * (TF32 operands split hi + lo, three products, FP32 accumulation in TMEM),
+ * and the CUDA cores run the rest of the adjoint.  tanh networks xd-16-16-1
+ * (fbp_has_tc_adjoint_shape); the same gradient partials up to FP32
+ * rounding.  Bounded waits as fbp_forward_pairs_tc (FBP_STATUS_TC_TIMEOUT in
+ * *status; FBP_STATUS_TC_TEST_NO_MMA exercises that path).
+ * Replaces XLA's reverse-mode transpose of the model (fbpinns/trainers.py:292). */
+int fbp_adjoint_pairs_tc(const fbp_net* net, const float* x, const fbp_pairs* pairs,
+                         const float* slot_out, float* grad_part, int32_t* status,
+                         int32_t grid, void* stream);
+
+/* 1 if fbp_adjoint_pairs_tc is compiled for this shape, jet mask and activation. */
+int fbp_has_tc_adjoint_shape(int32_t xd, int32_t h1, int32_t h2, int32_t d2mask, int32_t act);
+
 /* grad[j] = sum of the partials of subdomain j's items, in item order. */
 int fbp_grad_reduce(const float* grad_part, const int32_t* item_start, int64_t m,
                     int32_t nparam, float* grad, void* stream);

@@ -29,9 +29,9 @@ JET_TOL = 1e-5
 GRAD_TOL = 1e-5
 
 
-def _engine(static, layers, d2mask, chunk=64, activation="tanh", tensor_cores=None):
+def _engine(static, layers, d2mask, chunk=64, activation="tanh", tensor_cores=None, tc_adjoint=None):
     eng = FBPINNEngine(static, layer_sizes(layers), d2mask, chunk=chunk, activation=activation,
-                       tensor_cores=tensor_cores)
+                       tensor_cores=tensor_cores, tc_adjoint=tc_adjoint)
     eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
     return eng
 
@@ -192,15 +192,21 @@ def _bench_case(name, n):
     return _BENCH_ORACLE[(name, n)]
 
 
-@pytest.mark.parametrize("name,lap,tc,n", [("poisson_bench", True, True, 3000), ("poisson_bench", True, False, 3000),
-                                           ("poisson_bench", False, True, 3000), ("poisson_bench", False, False, 3000),
-                                           ("wave_bench", True, False, 1500), ("wave_bench", False, False, 1500)])
-def test_benchmarked_shapes_loss_and_gradient_vs_oracle(cuda, name, lap, tc, n):
+@pytest.mark.parametrize("name,lap,tc,tca,n", [("poisson_bench", True, True, False, 3000),
+                                               ("poisson_bench", True, False, False, 3000),
+                                               ("poisson_bench", False, True, False, 3000),
+                                               ("poisson_bench", False, False, False, 3000),
+                                               ("poisson_bench", True, True, True, 3000),
+                                               ("poisson_bench", False, True, True, 3000),
+                                               ("wave_bench", True, False, False, 1500),
+                                               ("wave_bench", False, False, False, 1500)])
+def test_benchmarked_shapes_loss_and_gradient_vs_oracle(cuda, name, lap, tc, tca, n):
     """The kernel instantiations that the benchmark and the full-size
     configurations run, at their real shapes, against the float64 oracle:
     Poisson 2-16-16-1 on the six-level decomposition (m = 1365) with the
     Laplacian slot (the benchmark's Cfg<2,16,16,11>) or per-dim slots
-    (Cfg<2,16,16,3>), tensor-core and FMA forward; the wave 3-32-32-1 on the
+    (Cfg<2,16,16,3>), tensor-core and FMA forward, tensor-core and FMA
+    adjoint; the wave 3-32-32-1 on the
     15x15x4 decomposition with its 12 sources, with the grouped u_xx + u_yy
     slot (Cfg<3,32,32,55>) or per-dim slots (Cfg<3,32,32,7>).  The
     benchmark's work-item sizes (1024 adjoint / 4096 forward pairs, cut for
@@ -209,8 +215,8 @@ def test_benchmarked_shapes_loss_and_gradient_vs_oracle(cuda, name, lap, tc, n):
     recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
     static, layers32, x, prob_static, (loss_ref, g_ref, a_ims, active) = _bench_case(name, n)
     d2e = d2 | (0 if not lap else _lib.D2_LAPLACIAN if d2 == 3 else _lib.D2_GROUP(3))
-    eng = _engine(static, layers32, d2e, chunk=1024, tensor_cores=tc)
-    assert eng.tensor_cores == tc and eng.forward_chunk == 4096
+    eng = _engine(static, layers32, d2e, chunk=1024, tensor_cores=tc, tc_adjoint=tca)
+    assert eng.tensor_cores == tc and eng.tc_adjoint == tca and eng.forward_chunk == 4096
     eng.set_state(active)
     eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
     ps = eng.points(torch.tensor(x))

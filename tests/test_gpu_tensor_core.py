@@ -150,3 +150,87 @@ def test_tensor_core_timeout_path_reports_and_recovers(cuda):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     _check(ref, ps.pair_out[:ps.s].clone(), eng.J)
+
+
+def _grads(recipe, d2, n, seed, tc_adjoint, problem="poisson", points=None):
+    """Per-subdomain gradient of the fused loss with the FMA or the
+    tensor-core adjoint (same forward, same seeds)."""
+    from fbpinns_gb300 import problems as PR
+    static = decomposition(recipe)
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = random_layers([2, 16, 16, 1], m, seed)
+    eng = FBPINNEngine(static, [2, 16, 16, 1], d2, chunk=512, tc_adjoint=tc_adjoint)
+    assert eng.tc_adjoint == tc_adjoint
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    if problem == "poisson":
+        spec = PR.Poisson2D.fused_spec({"static": {"problem": PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]}})
+    else:
+        spec = PR.BurgersEquation2D.fused_spec({"static": {"problem": PR.BurgersEquation2D.init_params()[0]}})
+    eng.set_problem(spec)
+    ps = eng.points(points if points is not None else torch.rand((n, 2), generator=torch.Generator().manual_seed(seed)))
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    ps.grad_part.fill_(float("nan"))
+    g = eng.adjoint(ps).clone()
+    torch.cuda.synchronize()
+    ps.check_status()
+    return loss, g
+
+
+@pytest.mark.parametrize("recipe,d2,n,problem", [("multilevel", 3 | 8, 3000, "poisson"),
+                                                 ("multilevel", 3, 3000, "poisson"),
+                                                 ("poisson", 3 | 8, 1 << 16, "poisson"),
+                                                 ("burgers", 1, 4000, "burgers")])
+def test_tensor_core_adjoint_matches_fma(cuda, recipe, d2, n, problem):
+    """The adjoint with the layer-2 recompute on the tensor cores gives the
+    FMA adjoint's gradients (every subdomain's, 2e-5 of the largest): the
+    benchmark's six-level Poisson shape with the Laplacian slot, per-dim
+    slots, and the Burgers jet (u_xx)."""
+    pts = None
+    if problem == "burgers":
+        g = torch.Generator().manual_seed(4)
+        pts = torch.stack([torch.rand(n, generator=g) * 2 - 1, torch.rand(n, generator=g)], 1)
+    l0, g0 = _grads(recipe, d2, n, 9, False, problem, pts)
+    l1, g1 = _grads(recipe, d2, n, 9, True, problem, pts)
+    assert l0 == l1  # the same forward and loss kernels
+    assert torch.isfinite(g1).all()
+    err = (g1 - g0).abs().max().item() / g0.abs().max().item()
+    assert err < TC_TOL, err
+
+
+def test_tensor_core_adjoint_timeout_path_reports_and_recovers(cuda):
+    """The tensor-core adjoint's bounded waits: with FBP_STATUS_TC_TEST_NO_MMA
+    no MMAs are issued, the waits (1 ms) run out, the kernel reports
+    FBP_STATUS_TC_TIMEOUT, frees its tensor memory and returns; the next
+    launch on the same context gives the FMA adjoint's gradient partials."""
+    from fbpinns_gb300 import problems as PR
+    static = decomposition("multilevel")
+    m = static["subdomain"]["params"][0].shape[0]
+    layers = random_layers([2, 16, 16, 1], m, 5)
+    eng = FBPINNEngine(static, [2, 16, 16, 1], 3 | 8, chunk=512)
+    eng.set_theta(pack_layers([(w.float(), b.float()) for w, b in layers]))
+    eng.set_problem(PR.Poisson2D.fused_spec({"static": {"problem": PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]}}))
+    ps = eng.points(torch.rand((3000, 2), generator=torch.Generator().manual_seed(2)))
+    eng.forward_pairs(ps)
+    eng.pou_loss(ps)
+    eng.adjoint(ps, reduce=False)
+    ref = ps.grad_part.clone()
+    lib = _lib.load()
+    net, pr = eng.net_struct(None), ps.pairs_struct(True)
+    status = torch.full((1,), 1 << 30, dtype=torch.int32, device=ps.x.device)  # FBP_STATUS_TC_TEST_NO_MMA
+    _lib.check(lib.fbp_adjoint_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
+                                        _lib.ptr(ps.grad_part), _lib.ptr(status), 0, _lib.stream_ptr()),
+               "fbp_adjoint_pairs_tc")
+    torch.cuda.synchronize()
+    assert int(status.item()) & 32  # FBP_STATUS_TC_TIMEOUT
+    status.zero_()
+    ps.grad_part.fill_(float("nan"))
+    _lib.check(lib.fbp_adjoint_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
+                                        _lib.ptr(ps.grad_part), _lib.ptr(status), 0, _lib.stream_ptr()),
+               "fbp_adjoint_pairs_tc")
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    n_items = int(ps.n_items_act.item())
+    a, b = ref[:n_items], ps.grad_part[:n_items]
+    assert torch.isfinite(b).all()
+    assert (a - b).abs().max().item() <= TC_TOL * a.abs().max().item()

@@ -196,3 +196,30 @@ def test_scheduler_changes_replay_one_capture(cuda):
     for a, b in zip(l_dev, l_host):
         assert abs(a - b) <= 1e-4 * abs(b), (a, b)
     assert abs(t_dev - t_host) <= 1e-4 * t_host
+
+
+def test_autotuner_searches_launches_and_caches(cuda, tmp_path, monkeypatch):
+    """The launch autotuner searches item sizes, schedule and both CTA
+    counts, keeps the fastest on the engine, and a second engine of the same
+    configuration takes the choice from the on-disk cache without timing."""
+    from fbpinns_gb300 import autotune
+    from fbpinns_gb300.engine import FBPINNEngine
+    from fbpinns_gb300.problems import Poisson2D
+    monkeypatch.setenv(autotune.CACHE_ENV, str(tmp_path / "tune.json"))
+    c = configs.poisson(n_steps=1, small=True)
+    dec = c.decomposition.init_params(**c.decomposition_init_kwargs)[0]
+    x = torch.rand((1 << 14, 2), generator=torch.Generator().manual_seed(3))
+    spec = Poisson2D.fused_spec({"static": {"problem": Poisson2D.init_params(n_freq=4, sd=0.1)[0]}})
+    out = []
+    for _ in range(2):
+        eng = FBPINNEngine(dec, [2, 16, 16, 1], 3 | 8)
+        eng.set_problem(spec)
+        out.append(autotune.tune_work_items(eng, x))
+    first, second = out
+    assert first["cache"] == "miss" and second["cache"] == "hit"
+    assert second["choice"] == first["choice"]
+    assert set(first["searched"]) == {"item_sizes", "schedule", "grid", "forward_grid"}
+    assert len(first["timings_ms"]) >= len(first["searched"]["item_sizes"]) + 2
+    ch = first["choice"]
+    assert (eng.chunk, eng.forward_chunk, eng.schedule, eng.launch_grid, eng.forward_grid) == \
+        (ch["chunk"], ch["forward_chunk"], ch["schedule"], ch["grid"], ch["forward_grid"])
