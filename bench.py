@@ -500,6 +500,7 @@ def run_fused(args, world, rank, local):
                 fstep.step()
             torch.cuda.synchronize()
             fstep.check()
+            match_tuned = getattr(eng4, "tuned", None)
             l1_fused = test_l1(eng4, problem, all_params, x_test, u_exact)
             l1_0 = test_l1_theta(eng4, theta0, problem, all_params, x_test, u_exact)
             del fstep, eng4
@@ -507,6 +508,7 @@ def run_fused(args, world, rank, local):
                      "fused_over_plain": ms_p / ms_max, "test_l1": l1_plain,
                      "matched": {"steps": k_match, "test_l1_initial": l1_0, "test_l1_fused": l1_fused,
                                  "test_l1_plain": l1_plain, "rel_gap": abs(l1_fused - l1_plain) / l1_plain,
+                                 "autotune_cache": match_tuned and match_tuned.get("cache"),
                                  "test_points": "100 x 100 grid on [0,1]^2"}}
         except Exception as ex:
             plain = {"value": None, "error": repr(ex)[:300]}
@@ -543,6 +545,41 @@ def run_fused(args, world, rank, local):
                 "cpu_baseline": cpu, "plain": plain, "test_l1": l1_fused, "loss_last": loss_last,
                 "evals_per_s": value * pairs}
         print(json.dumps(line), flush=True)
+
+
+def run_profile_plain(args):
+    """One plain GPU step of the workload under torch.profiler: the top
+    operations by CUDA time and the number of host synchronisations (one
+    JSON line, then the table)."""
+    from torch.profiler import ProfilerActivity, profile
+    from fbpinns_gb300.engine import FBPINNEngine
+    from fbpinns_gb300.optim import adam
+    from fbpinns_gb300.plain import PlainStep
+    dev = torch.device("cuda", 0)
+    static = decomposition_static()
+    problem, all_params = problem_setup()
+    eng = FBPINNEngine(static, LAYERS, d2mask=3, device=dev)
+    eng.set_theta(init_theta(static["m"]))
+    pstep = PlainStep(eng, problem, all_params, ((0, (0, 0)), (0, (1, 1))), adam(LR),
+                      resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], SEED))
+    for _ in range(2):
+        pstep.step()
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
+        t0 = time.perf_counter()
+        pstep.step()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ka = prof.key_averages()
+    dev_attr = "device_time_total" if hasattr(ka[0], "device_time_total") else "cuda_time_total"
+    top = sorted(ka, key=lambda e: getattr(e, dev_attr), reverse=True)[:25]
+    total = sum(getattr(e, "self_" + dev_attr, 0.0) for e in ka)
+    rows = [{"op": e.key, "calls": e.count, "device_ms": getattr(e, dev_attr) / 1000.0,
+             "self_device_ms": getattr(e, "self_" + dev_attr, 0.0) / 1000.0} for e in top]
+    syncs = sum(e.count for e in ka if e.key in ("aten::item", "aten::_local_scalar_dense"))
+    print(json.dumps({"metric": "plain step profile", "workload": WORKLOAD, "wall_ms": 1000 * wall,
+                      "self_device_ms_total": total / 1000.0, "host_reads": syncs, "top": rows}), flush=True)
+    print(ka.table(sort_by=dev_attr, row_limit=25), flush=True)
 
 
 def run_extras(args):
@@ -664,9 +701,14 @@ def main():
     ap.add_argument("--points", type=int, default=N_POINTS, help="collocation points per step")
     ap.add_argument("--extras", action="store_true",
                     help="instead of the bench line: other networks, inference and scheduler-change timings")
+    ap.add_argument("--profile-plain", action="store_true",
+                    help="instead of the bench line: one plain GPU step under torch.profiler")
     args = ap.parse_args()
     if args.extras:
         run_extras(args)
+        return
+    if args.profile_plain:
+        run_profile_plain(args)
         return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -17,11 +17,14 @@ points rather than guessed:
 The search is coordinate-wise: the item sizes first (dynamic schedule,
 resident grids), then the schedule, then the two CTA counts; every candidate
 builds the work queues for the points and times forward + POU/loss + adjoint
-with CUDA events.  The choice is kept on the engine and cached on disk, keyed
-by the GPU, the network, the jet, the subdomain count and the point and pair
-counts, so that a later run of the same configuration skips the search.  The
-candidates' results are identical up to the FP32 summation order of the
-per-item gradient partials.
+with CUDA events -- for a pipelined step with the next step's lists rebuilt
+on the higher-priority side stream at the same time, as in the step itself
+(the schedule decides how those list kernels get SMs during the jet
+kernels).  The choice is kept on the engine and cached on disk, keyed by the
+GPU, the network, the jet, the kernels, the subdomain and point counts and
+the pipelining, so that a later run of the same configuration skips the
+search.  The candidates' results are identical up to the FP32 summation
+order of the per-item gradient partials.
 """
 
 import json
@@ -42,13 +45,15 @@ def cache_path():
     return os.path.join(os.path.expanduser("~"), ".cache", "fbpinns_gb300", "autotune.json")
 
 
-def config_key(engine, n, s):
-    """The configuration a tuned launch is valid for (pair count to 3
-    significant digits: a redrawn batch of the same size keeps the key)."""
-    s3 = float(f"{float(s):.3g}")
+def config_key(engine, n, pipelined):
+    """The configuration a tuned launch is valid for: the GPU, the network and
+    its jet, the kernels used, the subdomain and point counts and whether the
+    next step's lists are built alongside (a redrawn batch of the same size
+    keeps the key; its pair count is recorded with the choice)."""
     props = torch.cuda.get_device_properties(engine.device)
     return "|".join(str(v) for v in (props.name, props.multi_processor_count, engine.layer_sizes, engine.activation,
-                                     engine.d2mask, int(engine.tensor_cores), engine.m, int(n), s3))
+                                     engine.d2mask, int(engine.tensor_cores), int(getattr(engine, "tc_adjoint", 0)),
+                                     engine.m, int(n), int(bool(pipelined))))
 
 
 def _load_cache(path):
@@ -60,7 +65,9 @@ def _load_cache(path):
 
 
 def _store_cache(path, key, entry):
-    """Adds one entry (atomic replace: readers never see a partial file)."""
+    """Adds one entry (atomic replace: readers never see a partial file).
+    Returns None, or the reason the file could not be written (the choice
+    still holds for this run)."""
     try:
         os.makedirs(os.path.dirname(path), exist_ok=True)
         data = _load_cache(path)
@@ -69,8 +76,9 @@ def _store_cache(path, key, entry):
         with os.fdopen(fd, "w") as f:
             json.dump(data, f, indent=1, sort_keys=True)
         os.replace(tmp, path)
-    except OSError:
-        pass  # a read-only home: the choice still holds for this run
+        return None
+    except OSError as ex:
+        return repr(ex)
 
 
 def default_candidates(s, m, sms):
@@ -95,25 +103,40 @@ def _apply(engine, choice):
     engine.adaptive_items = False
 
 
-def _pass(engine, ps):
+def _pass(engine, ps, side=None):
+    """The step's device work on point set ps.  With side = (stream, point
+    set), that set's lists are rebuilt on the (higher-priority) stream at
+    the same time, as the pipelined step builds the next step's lists."""
+    main = torch.cuda.current_stream()
+    if side is not None:
+        stream, ps2 = side
+        stream.wait_stream(main)
+        with torch.cuda.stream(stream):
+            ps2.rebuild(stream=stream)
     engine.forward_pairs(ps)
     engine.pou_loss(ps)
     engine.adjoint(ps)
+    if side is not None:
+        main.wait_stream(side[0])
 
 
-def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=True):
+def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=True, pipelined=False):
     """Tune the launches of the step's device work on points x and set the
     choice on the engine (``chunk``, ``forward_chunk``, ``schedule``,
     ``launch_grid``, ``forward_grid``).  Needs ``engine.set_problem`` first.
-    Returns (and keeps as ``engine.tuned``) the choice, what was searched,
-    every candidate's time in ms and whether the cache held the answer."""
+    ``pipelined``: time each candidate with the lists of a second point set
+    rebuilt on a higher-priority stream alongside (the pipelined step's
+    load).  Returns (and keeps as ``engine.tuned``) the choice, what was
+    searched, every candidate's time in ms and whether the cache held it."""
     x = torch.as_tensor(x, dtype=torch.float32).to(engine.device)
     probe = engine.points(x)
     s, n = probe.s, probe.n
     if candidates is None:
         candidates = default_candidates(s, engine.m, engine.sm_count)
+    if pipelined and caps is None:
+        caps = (int(probe.s * 1.25) + 1024, int(probe.u * 1.25) + 1024)
     del probe
-    key = config_key(engine, n, s)
+    key = config_key(engine, n, pipelined)
     path = cache_path()
     if use_cache:
         hit = _load_cache(path).get(key)
@@ -126,6 +149,8 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
                 "grid": [0, sms, 2 * sms, 3 * sms], "forward_grid": [0, sms, 2 * sms]}
     timings = {}
     ev = lambda: torch.cuda.Event(enable_timing=True)
+    if pipelined:
+        side_stream = torch.cuda.Stream(device=engine.device, priority=-1)
 
     def run(choice):
         tag = f"{choice['chunk']}/{choice['forward_chunk']} {choice['schedule']} g{choice['grid']} " \
@@ -134,16 +159,17 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
             return timings[tag]
         _apply(engine, choice)
         ps = engine.points(x, caps=caps)
-        _pass(engine, ps)  # warm-up: per-device kernel attributes, caches
+        side = (side_stream, engine.points(x, caps=caps)) if pipelined else None
+        _pass(engine, ps, side)  # warm-up: per-device kernel attributes, caches
         torch.cuda.synchronize()
         a, b = ev(), ev()
         a.record()
         for _ in range(reps):
-            _pass(engine, ps)
+            _pass(engine, ps, side)
         b.record()
         torch.cuda.synchronize()
         ps.check_status()
-        del ps
+        del ps, side
         timings[tag] = a.elapsed_time(b) / reps
         return timings[tag]
 
@@ -163,9 +189,10 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
             if best_t is None or t < best_t:
                 best, best_t = c, t
     _apply(engine, best)
-    entry = {"choice": best, "searched": searched, "best_ms": round(best_t, 4),
-             "timings_ms": {k: round(v, 4) for k, v in timings.items()}}
-    if use_cache:
-        _store_cache(path, key, entry)
+    entry = {"choice": best, "searched": searched, "best_ms": round(best_t, 4), "pairs": int(s),
+             "pipelined": bool(pipelined), "timings_ms": {k: round(v, 4) for k, v in timings.items()}}
+    err = _store_cache(path, key, entry) if use_cache else None
     engine.tuned = dict(entry, cache="miss", key=key)
+    if err:
+        engine.tuned["cache_write_error"] = err
     return engine.tuned

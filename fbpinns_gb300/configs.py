@@ -121,9 +121,15 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--engine", default="fused", choices=["fused", "plain"])
     ap.add_argument("--small", action="store_true")
+    ap.add_argument("--layers", default=None, help="network layer sizes, e.g. 1,32,1 (default: the config's)")
+    ap.add_argument("--test-every", type=int, default=0, help="steps between test-L1 evaluations (default n/5)")
     a = ap.parse_args()
     c = CONFIGS[a.config](n_steps=a.steps, small=a.small)
     c.engine = a.engine
+    if a.layers:
+        c.network_init_kwargs = dict(c.network_init_kwargs, layer_sizes=[int(v) for v in a.layers.split(",")])
+    if a.test_every:
+        c.test_freq = a.test_every
     tr = FBPINNTrainer(c)
     t0 = time.time()
     tr.train()
@@ -131,6 +137,8 @@ def main():
     wall = time.time() - t0
     rates = [h["rate"] for h in tr.history[1:]] or [h["rate"] for h in tr.history]
     print(json.dumps({"config": a.config, "engine": a.engine, "steps": a.steps, "small": a.small,
+                      "layers": c.network_init_kwargs["layer_sizes"],
+                      "test_l1_normalised": [r[2] for r in tr.u_test_losses],
                       "wall_s": round(wall, 2), "steps_per_s": float(np.median(rates)) if rates else None,
                       "test_l1": [r[1] for r in tr.u_test_losses], "test_l1_steps": [r[0] for r in tr.u_test_losses],
                       "loss": [h["loss"] for h in tr.history]}))

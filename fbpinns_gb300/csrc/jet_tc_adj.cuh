@@ -19,9 +19,9 @@
 // Phases B and C, the W3/W1/bias reduce-scatters and the per-item gradient
 // partials are those of adjoint_pairs_kernel (jet.cuh); the z-jets come from
 // the tensor cores instead of FFMA2 loops, so the CUDA cores drop a third of
-// their layer-2 FMAs.  Two CTAs share an SM (about 109 KB of shared memory
-// each), so one CTA's CUDA-core phases run while the other waits for its
-// MMAs.  Waits on the MMA-completion mbarrier are bounded as in the forward
+// their layer-2 FMAs.  Three CTAs share an SM (about 74 KB of shared memory
+// each: the z2-bar rows reuse the A-operand region), so CUDA-core phases run
+// while other CTAs wait for their MMAs.  Waits on the MMA-completion mbarrier are bounded as in the forward
 // kernel: on a time-out the CTA records FBP_STATUS_TC_TIMEOUT, stops, waits
 // once more and frees its TMEM.
 #pragma once
@@ -42,10 +42,12 @@ struct TcAdjSmem {
     uint32_t pad_;
 };
 
-// One warp's rows and gradient sums (the warp owns 32 lanes = pairs of a tile).
+// One warp's rows and gradient sums (the warp owns 32 lanes = pairs of a
+// tile).  Its z2-bar rows live in the A-operand region of TcAdjSmem: they are
+// written after the tile's MMAs have completed and read before the next tile
+// is staged, so the two never hold data at the same time.
 template <class C>
 struct __align__(16) TcAdjWarp {
-    float zb[32 * AdjW<C>::ZS];  // z2-bar rows [t][c][k]
     float a1[32 * AdjW<C>::AS];  // layer-1 activations [t][n]
     float gW2[C::H2 * C::H1];
     float gW1[C::H1 * C::XD];
@@ -58,8 +60,8 @@ struct __align__(16) TcAdjWarp {
 // Phase B of one warp tile: v-bar = W2^T z2-bar (own row), the layer-1 jet
 // adjoint, and the W1-bar / b1-bar terms summed over the warp.
 template <class C>
-__device__ __forceinline__ void tc_adj_phase_b(const SParams<C>& S, TcAdjWarp<C>& R, const float* a1row, bool act,
-                                               const float (&xn)[C::XD], int lane) {
+__device__ __forceinline__ void tc_adj_phase_b(const SParams<C>& S, TcAdjWarp<C>& R, const float* zb,
+                                               const float* a1row, bool act, const float (&xn)[C::XD], int lane) {
     using A = AdjW<C>;
     constexpr int J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2;
     constexpr int RN = XD + 1;
@@ -76,7 +78,7 @@ __device__ __forceinline__ void tc_adj_phase_b(const SParams<C>& S, TcAdjWarp<C>
             for (int q = 0; q < NC / 2; ++q)
 #pragma unroll
                 for (int c = 0; c < J; ++c) vb2[q][c] = make_float2(0.f, 0.f);
-            const float* zrow = &R.zb[lane * A::ZS];
+            const float* zrow = zb + lane * A::ZS;
 #pragma unroll 1
             for (int k0 = 0; k0 < H2; k0 += 4) {
                 float4 z4[J];
@@ -138,8 +140,8 @@ __device__ __forceinline__ void tc_adj_phase_b(const SParams<C>& S, TcAdjWarp<C>
 // Phase C of one warp tile: W2-bar and b2-bar over its nt pairs (lane = a
 // KB x NB block of W2-bar; rows in pairs share packed FMAs).
 template <class C>
-__device__ __forceinline__ void tc_adj_phase_c(const SParams<C>& S, TcAdjWarp<C>& R, const float* a1rows, int nt,
-                                               int lane) {
+__device__ __forceinline__ void tc_adj_phase_c(const SParams<C>& S, TcAdjWarp<C>& R, const float* zb,
+                                               const float* a1rows, int nt, int lane) {
     using A = AdjW<C>;
     constexpr int J = C::J, XD = C::XD, H1 = C::H1, H2 = C::H2;
 #pragma unroll 1
@@ -170,7 +172,7 @@ __device__ __forceinline__ void tc_adj_phase_c(const SParams<C>& S, TcAdjWarp<C>
                 m[q][1] = tp;
                 m[q][2] = tpp;
             }
-            const float* zr = &R.zb[t * A::ZS + k0];
+            const float* zr = zb + t * A::ZS + k0;
 #pragma unroll
             for (int c = 0; c < J; ++c) {
                 float2 z2[A::KB / 2];
@@ -231,6 +233,7 @@ __global__ void __launch_bounds__(TC_TILE) adjoint_pairs_tc_kernel(fbp_net net, 
     constexpr int J = C::J, XD = C::XD, H1 = 16, H2 = 16, RS = rec_stride(J);
     constexpr int NA = TcAdjSmem<C>::NA;
     static_assert(sizeof(TcAdjWarp<C>) % 16 == 0 && A::ZS % 4 == 0, "16-byte rows");
+    static_assert((TC_TILE / 32) * 32 * A::ZS <= (int)sizeof(TcAdjSmem<C>::a) / 4, "z2-bar rows fit the A region");
     __shared__ SParams<C> S;
     extern __shared__ float4 dyn_smem[];
     TcAdjSmem<C>& T = *reinterpret_cast<TcAdjSmem<C>*>(dyn_smem);
@@ -238,6 +241,7 @@ __global__ void __launch_bounds__(TC_TILE) adjoint_pairs_tc_kernel(fbp_net net, 
                                                        ((sizeof(TcAdjSmem<C>) + 15) / 16) * 16);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     TcAdjWarp<C>& R = RW[warp];
+    float* zb = &T.a[0][0][0] + warp * 32 * A::ZS;  // this warp's z2-bar rows (in the A region)
     const uint32_t mbar = smem_u32(&T.mbar);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
@@ -303,6 +307,9 @@ __global__ void __launch_bounds__(TC_TILE) adjoint_pairs_tc_kernel(fbp_net net, 
 #pragma unroll
             for (int c = 0; c < J; ++c) ob[c] = 0.f;
             float* a1row = &R.a1[lane * A::AS];
+            // every warp has read its z2-bar rows (the previous tile's phase C)
+            // before the A operands overwrite that region
+            __syncthreads();
             // ---- stage A: seeds -> o-bar; layer 1 -> A operands and a1 row ----
             if (act) {
                 float w[J];
@@ -400,7 +407,7 @@ __global__ void __launch_bounds__(TC_TILE) adjoint_pairs_tc_kernel(fbp_net net, 
                     tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), acc[c]);
                 tmem_wait_ld();
                 float e3[16];
-                float* zrow = &R.zb[lane * A::ZS];
+                float* zrow = zb + lane * A::ZS;
 #pragma unroll
                 for (int k = 0; k < H2; k += 2) {
                     float2 z[J];
@@ -467,8 +474,8 @@ __global__ void __launch_bounds__(TC_TILE) adjoint_pairs_tc_kernel(fbp_net net, 
             }
             __syncwarp();  // z2-bar and a1 rows of the warp's pairs are written
             // ---- phases B and C (warp-level) ----
-            tc_adj_phase_b<C>(S, R, a1row, act, xn, lane);
-            tc_adj_phase_c<C>(S, R, R.a1, nt, lane);
+            tc_adj_phase_b<C>(S, R, zb, a1row, act, xn, lane);
+            tc_adj_phase_c<C>(S, R, zb, R.a1, nt, lane);
             __syncwarp();  // every lane has read the rows before the next tile rewrites them
         }
         if (failed) break;

@@ -172,15 +172,18 @@ class FusedStep:
         self.scheduled = bool(scheduled)
         engine.set_problem(spec)
         if autotune:
-            # work-item sizes measured on this step's first batch of points
+            # launches measured on this step's first batch of points (with the next
+            # step's lists built alongside when the step is pipelined)
             from .autotune import tune_work_items
             if resample is not None:
                 xt = torch.empty((resample[0], engine.xd), dtype=torch.float32, device=engine.device)
                 engine.sample(xt, int(resample[3]), 1 << 32, list(resample[1]), list(resample[2]))
             else:
                 xt = x_probe if host_points is not None else x
+            piped = (resample is not None or host_points is not None) and \
+                (bool(pipeline) if pipeline is not None else resample is not None)
             if xt is not None:
-                tune_work_items(engine, xt)
+                tune_work_items(engine, xt, pipelined=piped)
         self.resample = resample
         self.host = host_points is not None
         self.use_graph = use_graph

@@ -695,16 +695,22 @@ def test_work_item_autotuner(cuda):
     eng = _engine(static, layers, 3 | _lib.D2_LAPLACIAN, chunk=1024)
     eng.set_problem(spec)
     cands = [(256, 256), (256, 1024), (512, 2048)]
-    tuned = tune_work_items(eng, x, candidates=cands)
-    assert set(tuned["timings_ms"]) == {f"{a}/{f}" for a, f in cands}
-    best = min(cands, key=lambda c: tuned["timings_ms"][f"{c[0]}/{c[1]}"])
-    assert (eng.chunk, eng.forward_chunk) == best == (tuned["chunk"], tuned["forward_chunk"])
+    tuned = tune_work_items(eng, x, candidates=cands, use_cache=False)
+    sizes = {f"{a}/{f} dynamic g0 fg0": (a, f) for a, f in cands}
+    assert set(sizes) <= set(tuned["timings_ms"])
+    best_size = min(sizes, key=lambda k: tuned["timings_ms"][k])
+    ch = tuned["choice"]
+    best = (ch["chunk"], ch["forward_chunk"])
+    assert best == sizes[best_size]  # later stages tune the schedule and grids at these sizes
+    assert tuned["best_ms"] == min(tuned["timings_ms"].values())
+    assert (eng.chunk, eng.forward_chunk) == best
     ps = eng.points(x)
     assert (ps.chunk, ps.fwd_chunk) == best
     eng.forward_pairs(ps)
     loss = eng.pou_loss(ps).item()
     ref = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=best[0], forward_chunk=best[1],
-                       adaptive_items=False)
+                       adaptive_items=False, schedule=ch["schedule"], grid=ch["grid"])
+    ref.forward_grid = ch["forward_grid"]
     ref.set_theta(eng.theta.clone())
     ref.set_problem(spec)
     ps2 = ref.points(x)

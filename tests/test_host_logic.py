@@ -509,3 +509,31 @@ def test_wave_field_matches_reference_cpml_solver():
         d = np.abs(u[..., k] - ur[..., k])
         assert d.mean() < 0.012 * np.abs(ur[..., k]).mean(), k
         assert d.max() < 0.02 * np.abs(ur).max(), k
+
+
+def test_helmholtz_reference_field_convergence():
+    """The finite-difference field of the Helmholtz problem (helmholtz_fd.py),
+    grid n against 2n on interior points.  Off resonance (k = 3 pi) it
+    converges at second order (the difference falls 4x per halving of h).
+    At k = 40 pi -- a Dirichlet eigenvalue of the unit square, since
+    24^2 + 32^2 = 40^2 -- it does not converge (differences of the order of
+    the field): -lap u - k^2 u = f with u = 0 on the boundary has no solution
+    for a generic f there, so no test error can be defined for that k."""
+    from fbpinns_gb300.helmholtz_fd import helmholtz_grid
+    from fbpinns_gb300.problems import seeded_gaussians
+    from fbpinns_gb300.wave_fd import bilinear
+    src = seeded_gaussians(8, 1, width=(0.05, 0.1))
+    g = np.linspace(0.05, 0.95, 46)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+
+    def diffs(k, ns):
+        v = {}
+        for n in ns:
+            xs, U = helmholtz_grid(k, src, n)
+            v[n] = bilinear(xs, xs, U, X.ravel(), Y.ravel())
+        return [np.abs(v[a] - v[b]).mean() / np.abs(v[b]).mean() for a, b in zip(ns[:-1], ns[1:])]
+
+    e = diffs(3 * math.pi, (100, 200, 400))
+    assert e[1] < 1e-3 and 3.5 < e[0] / e[1] < 4.5, e
+    r = diffs(40 * math.pi, (200, 400, 800))
+    assert min(r) > 0.3, r
