@@ -548,10 +548,10 @@ def run_fused(args, world, rank, local):
 
 
 def run_profile_plain(args):
-    """One plain GPU step of the workload under torch.profiler: the top
-    operations by CUDA time and the number of host synchronisations (one
-    JSON line, then the table)."""
-    from torch.profiler import ProfilerActivity, profile
+    """One plain GPU step of the workload between cudaProfilerStart and
+    cudaProfilerStop (after two warm-up steps), for a launch list of exactly
+    that step: ``ncu --profile-from-start off --metrics gpu__time_duration.sum
+    ... python bench.py --profile-plain``.  Prints the step's wall time."""
     from fbpinns_gb300.engine import FBPINNEngine
     from fbpinns_gb300.optim import adam
     from fbpinns_gb300.plain import PlainStep
@@ -565,21 +565,13 @@ def run_profile_plain(args):
     for _ in range(2):
         pstep.step()
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
-        t0 = time.perf_counter()
-        pstep.step()
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    ka = prof.key_averages()
-    dev_attr = "device_time_total" if hasattr(ka[0], "device_time_total") else "cuda_time_total"
-    top = sorted(ka, key=lambda e: getattr(e, dev_attr), reverse=True)[:25]
-    total = sum(getattr(e, "self_" + dev_attr, 0.0) for e in ka)
-    rows = [{"op": e.key, "calls": e.count, "device_ms": getattr(e, dev_attr) / 1000.0,
-             "self_device_ms": getattr(e, "self_" + dev_attr, 0.0) / 1000.0} for e in top]
-    syncs = sum(e.count for e in ka if e.key in ("aten::item", "aten::_local_scalar_dense"))
-    print(json.dumps({"metric": "plain step profile", "workload": WORKLOAD, "wall_ms": 1000 * wall,
-                      "self_device_ms_total": total / 1000.0, "host_reads": syncs, "top": rows}), flush=True)
-    print(ka.table(sort_by=dev_attr, row_limit=25), flush=True)
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    pstep.step()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    torch.cuda.profiler.stop()
+    print(json.dumps({"metric": "plain step", "workload": WORKLOAD, "wall_ms": 1000 * wall}), flush=True)
 
 
 def run_extras(args):
@@ -702,7 +694,7 @@ def main():
     ap.add_argument("--extras", action="store_true",
                     help="instead of the bench line: other networks, inference and scheduler-change timings")
     ap.add_argument("--profile-plain", action="store_true",
-                    help="instead of the bench line: one plain GPU step under torch.profiler")
+                    help="instead of the bench line: one plain GPU step bracketed for a profiler launch list")
     args = ap.parse_args()
     if args.extras:
         run_extras(args)

@@ -34,6 +34,21 @@ def ho(n_steps=10000, small=False):
                      summary_freq=max(1, n_steps // 10), test_freq=max(1, n_steps // 5))
 
 
+def ho_example(n_steps=20000, small=False):
+    """The reference's own hard-constraint oscillator example
+    (examples/2. Using hard constraints - 1D harmonic oscillator.ipynb):
+    d=2, w0=80, 15 subdomains of width 0.15, FCN 1-32-1, 200 grid points,
+    Adam 1e-3, 20,000 steps, test on 500 points -- the run behind the
+    README's FBPINN test-loss curve."""
+    c = ho(n_steps=n_steps, small=small)
+    c.run = "ho_example"
+    c.decomposition_init_kwargs = dict(subdomain_xs=[np.linspace(0, 1, 15)], subdomain_ws=[0.15 * np.ones((15,))],
+                                       unnorm=(0., 1.))
+    c.network_init_kwargs = dict(layer_sizes=[1, 32, 1])
+    c.n_test = (500,)
+    return c
+
+
 def burgers(n_steps=10000, small=False):
     """(1+1)D viscous Burgers: 16x8 subdomains (width 2.9x spacing), FCN
     2-16-16-1, 200x200 grid, line scheduler from x=0 along t."""
@@ -110,7 +125,8 @@ def helmholtz(n_steps=10000, small=False):
                      summary_freq=max(1, n_steps // 10), test_freq=max(1, n_steps // 5))
 
 
-CONFIGS = {"ho": ho, "burgers": burgers, "poisson": poisson, "wave": wave, "helmholtz": helmholtz}
+CONFIGS = {"ho": ho, "ho_example": ho_example, "burgers": burgers, "poisson": poisson, "wave": wave,
+           "helmholtz": helmholtz}
 
 
 def main():

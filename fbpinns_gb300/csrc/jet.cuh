@@ -602,6 +602,20 @@ struct AdjW {
     static_assert(KB == 2 || KB == 4 || KB == 8, "W2-bar rows per lane");
 };
 
+// Phase B's layer-1 chunks: NC neurons per reduce-scatter of 32 values, RN
+// values each (W1-bar row, b1-bar, activation parameters).  When the
+// remaining slots hold NB2 values per chunk (in 4-aligned runs), b2-bar rides
+// in them (B2_IN_B) instead of being summed per pair in phase C.
+template <class C>
+struct AdjB {
+    static constexpr int RN = C::XD + 1 + C::EXTRA;
+    static constexpr int NCF = 32 / RN >= 8 ? 8 : (32 / RN >= 4 ? 4 : 2);
+    static constexpr int NC = NCF < C::H1 ? NCF : C::H1;
+    static constexpr int NB2 = C::TWO ? C::H2 * NC / C::H1 : 0;
+    static constexpr bool B2_IN_B =
+        C::TWO && NB2 > 0 && NB2 % 4 == 0 && NC * RN + NB2 <= 32 && (C::H2 * NC) % C::H1 == 0;
+};
+
 // One warp's rows; 16-byte aligned so that every warp's z2-bar rows (read and
 // written as float4) start on a 16-byte boundary in the array of WarpRows.
 template <class C>
@@ -808,9 +822,8 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
             // ---------------- phase B: layer-1 adjoint ----------------
             // per chunk of NC first-layer neurons: v-bar = W2^T z2-bar (own row), the
             // layer-1 jet adjoint, and the W1-bar / b1-bar terms summed over the warp
-            constexpr int RN = XD + 1 + C::EXTRA;  // reduced values per neuron: W1-bar row, b1-bar, parameters
-            constexpr int NCF = 32 / RN >= 8 ? 8 : (32 / RN >= 4 ? 4 : 2);
-            constexpr int NC = NCF < H1 ? NCF : H1;
+            constexpr int RN = AdjB<C>::RN, NC = AdjB<C>::NC, NB2 = AdjB<C>::NB2;
+            constexpr bool B2_IN_B = AdjB<C>::B2_IN_B;  // b2-bar rides in the free slots
             static_assert(NC * RN <= 32 && H1 % NC == 0, "layer-1 chunk must fit one reduce-scatter");
 #pragma unroll 1
             for (int n0 = 0; n0 < H1; n0 += NC) {
@@ -894,6 +907,18 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                             for (int x = 0; x < C::EXTRA; ++x) r1[q * RN + XD + 1 + x] = pg[x];
                         }
                     }
+                    if constexpr (B2_IN_B) {  // this chunk's b2-bar terms: z2-bar_0 of NB2 neurons
+                        const float* zrow = &R.zb[lane * A::ZS];
+                        const int kb0 = (n0 / NC) * NB2;
+#pragma unroll
+                        for (int i = 0; i < NB2; i += 4) {
+                            const float4 z4 = *reinterpret_cast<const float4*>(zrow + kb0 + i);
+                            r1[NC * RN + i] = z4.x;
+                            r1[NC * RN + i + 1] = z4.y;
+                            r1[NC * RN + i + 2] = z4.z;
+                            r1[NC * RN + i + 3] = z4.w;
+                        }
+                    }
                 }
                 warp_reduce_scatter<32>(r1, lane);
                 if (lane < NC * RN) {
@@ -904,9 +929,13 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                         R.gb1[n0 + q] += r1[0];
                     else if constexpr (C::EXTRA > 0)
                         R.gX1[(d - XD - 1) * H1 + n0 + q] += r1[0];
+                } else if (B2_IN_B && lane < NC * RN + NB2) {
+                    R.gb2[(n0 / NC) * NB2 + lane - NC * RN] += r1[0];
                 }
             }
             // ---------------- phase C: W2-bar over the tile ----------------
+            // (b2-bar here only when phase B's reduce-scatters have no room for it)
+            constexpr bool B2_IN_C = !AdjB<C>::B2_IN_B;
             if constexpr (C::TWO) {
 #pragma unroll 1
                 for (int ps = 0; ps < A::PASSES; ++ps) {
@@ -953,7 +982,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                     }
                                 }
                                 const int mi = c == 0 ? 0 : (c <= XD ? 1 : 2);
-                                if (c == 0) {
+                                if (B2_IN_C && c == 0) {
 #pragma unroll
                                     for (int i = 0; i < A::KB / 2; ++i) {
                                         b2s[2 * i] += z2[i].x;
@@ -984,7 +1013,7 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                                     v = fmaf(S.c2[n * C::NS + ss], s[1 + XD + ss], v);
                                 R.gW2[(k0 + i) * H1 + n] += v;
                             }
-                        if (nb == 0) {
+                        if (B2_IN_C && nb == 0) {
 #pragma unroll
                             for (int i = 0; i < A::KB; ++i) R.gb2[k0 + i] += b2s[i];
                         }
