@@ -40,6 +40,8 @@ ACT_TANH, ACT_SIN, ACT_ADAPTIVE_TANH, ACT_ADAPTIVE_SIN, ACT_FOURIER = 0, 1, 2, 3
 ACTIVATIONS = {"tanh": ACT_TANH, "sin": ACT_SIN, "adaptive_tanh": ACT_ADAPTIVE_TANH, "adaptive_sin": ACT_ADAPTIVE_SIN,
                "fourier": ACT_FOURIER}
 ACT_EXTRA = {"tanh": 0, "sin": 0, "adaptive_tanh": 1, "adaptive_sin": 2, "fourier": 0}
+# FBP_WINDOW_*: the subdomain window (fbpinns/windows.py)
+WINDOW_COSINE, WINDOW_SIGMOID, WINDOW_BUMP, WINDOW_WENDLAND, WINDOW_RBF = range(5)
 
 
 class FBPLibraryError(RuntimeError):
@@ -55,7 +57,8 @@ class Boxes(C.Structure):
 class Net(C.Structure):
     _fields_ = [("xd", C.c_int32), ("h1", C.c_int32), ("h2", C.c_int32), ("ud", C.c_int32), ("d2mask", C.c_int32),
                 ("nparam", C.c_int32), ("act", C.c_int32), ("theta", C.c_void_p), ("xmins", C.c_void_p), ("xmaxs", C.c_void_p),
-                ("flags", C.c_void_p), ("unnorms", C.c_void_p), ("m", C.c_int64)]
+                ("flags", C.c_void_p), ("unnorms", C.c_void_p), ("m", C.c_int64), ("window", C.c_int32),
+                ("wmins", C.c_void_p), ("wmaxs", C.c_void_p)]
 
 
 class Pairs(C.Structure):

@@ -186,7 +186,10 @@ struct SParams {
     float ac1[C::EXTRA > 0 ? C::H1 : 1], ao1[C::EXTRA > 0 ? C::H1 : 1];
     float ac2[C::EXTRA > 0 && C::TWO ? C::H2 : 1], ao2[C::EXTRA > 0 && C::TWO ? C::H2 : 1];
     float mu[C::XD], inv_sd[C::XD], wsc[C::XD];  // wsc = pi / (2 sd)
+    // sigmoid window per dim: a = sg0 + sg1 xn, b = sg2 - sg3 xn (window_1d)
+    float sg[C::XD][4];
     float flag, mu_u, sd_u;
+    int window;
 };
 
 // the (c, o) of hidden neuron n of layer 1 (L2 = false) or 2 (L2 = true)
@@ -235,6 +238,7 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
     }
     if (threadIdx.x == 0) {
         S.b3 = th[C::ob3];
+        S.window = net.window;
         S.flag = net.flags[j];
         S.mu_u = net.unnorms[2 * (size_t)j];
         S.sd_u = net.unnorms[2 * (size_t)j + 1];
@@ -246,6 +250,17 @@ __device__ __forceinline__ void load_params(SParams<C>& S, const fbp_net& net, i
         S.mu[d] = (hi + lo) / 2.0f;
         S.inv_sd[d] = 1.0f / sd;
         S.wsc[d] = 1.5707963267948966f / sd;
+        if (net.window == FBP_WINDOW_SIGMOID) {
+            // ramps of fbpinns/windows.py:11-22 with t = log((1 - tol) / tol), tol = 1e-8:
+            // a = (x - mu_min) / sd_min, b = (mu_max - x) / sd_max, written in xn = (x - mu) / sd
+            const float t = 18.420680743952367f;
+            const float wlo = net.wmins[(size_t)j * C::XD + d], whi = net.wmaxs[(size_t)j * C::XD + d];
+            const float ia = 2.0f * t / wlo, ib = 2.0f * t / whi;
+            S.sg[d][0] = (S.mu[d] - (lo + wlo / 2.0f)) * ia;  // a at xn = 0
+            S.sg[d][1] = sd * ia;                             // da / dxn
+            S.sg[d][2] = ((hi - whi / 2.0f) - S.mu[d]) * ib;  // b at xn = 0
+            S.sg[d][3] = sd * ib;                             // -db / dxn
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < C::H1 * C::XD; i += blockDim.x) {
@@ -326,19 +341,64 @@ __device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float tp, f
 
 // Window jet (cosine window of fbpinns/windows.py:25-35 times flag plus 1-flag):
 // per dim c = cos^4(phi), phi = (pi/2) xn; derivatives by the chain rule.
+// The 1D window of dim d at the normalised coordinate xn and its first two
+// derivatives with respect to x (inv_sd = dxn/dx); the window kind is the
+// same for every thread of a launch.
+template <class C>
+__device__ __forceinline__ void window_1d(const SParams<C>& S, int d, float xn, float& c0, float& c1, float& c2) {
+    const float is = S.inv_sd[d];
+    switch (S.window) {
+        case FBP_WINDOW_SIGMOID: {  // A(a) B(b), A = B = logistic, a' = sa1 is, b' = -sb1 is
+            const float a = fmaf(S.sg[d][1], xn, S.sg[d][0]), b = fmaf(-S.sg[d][3], xn, S.sg[d][2]);
+            const float A = 1.0f / (1.0f + __expf(-a)), B = 1.0f / (1.0f + __expf(-b));
+            const float ka = S.sg[d][1] * is, kb = S.sg[d][3] * is;
+            const float A1 = A * (1.0f - A) * ka, A2 = A * (1.0f - A) * (1.0f - 2.0f * A) * ka * ka;
+            const float B1 = -B * (1.0f - B) * kb, B2 = B * (1.0f - B) * (1.0f - 2.0f * B) * kb * kb;
+            c0 = A * B;
+            c1 = A1 * B + A * B1;
+            c2 = A2 * B + 2.0f * A1 * B1 + A * B2;
+            break;
+        }
+        case FBP_WINDOW_BUMP: {  // e = exp(3 / q + 3), q = xn^2 - 1.001
+            const float q = xn * xn - 1.001f, iq = 1.0f / q;
+            const float e = __expf(fmaf(3.0f, iq, 3.0f));
+            const float h1 = -6.0f * xn * iq * iq, h2 = (-6.0f + 24.0f * xn * xn * iq) * iq * iq;
+            c0 = e;
+            c1 = e * h1 * is;
+            c2 = e * (h2 + h1 * h1) * is * is;
+            break;
+        }
+        case FBP_WINDOW_WENDLAND: {  // (1 - r)^4 (4 r + 1), r = |xn|
+            const float r = fabsf(xn), om = 1.0f - r, om2 = om * om;
+            c0 = om2 * om2 * (4.0f * r + 1.0f);
+            c1 = -20.0f * xn * om2 * om * is;
+            c2 = 20.0f * om2 * (4.0f * r - 1.0f) * is * is;
+            break;
+        }
+        case FBP_WINDOW_RBF: {  // exp(-0.5 (xn / 0.25)^2) = exp(-8 xn^2)
+            const float g = __expf(-8.0f * xn * xn);
+            c0 = g;
+            c1 = -16.0f * xn * g * is;
+            c2 = (256.0f * xn * xn - 16.0f) * g * is * is;
+            break;
+        }
+        default: {  // cosine: cos^4(phi), phi = pi xn / 2
+            float sn, cs;
+            sincosf(1.5707963267948966f * xn, &sn, &cs);
+            const float cs2 = cs * cs;
+            const float k = S.wsc[d];
+            c0 = cs2 * cs2;
+            c1 = -4.0f * cs2 * cs * sn * k;
+            c2 = (12.0f * cs2 * sn * sn - 4.0f * cs2 * cs2) * k * k;
+        }
+    }
+}
+
 template <class C>
 __device__ __forceinline__ void window_jet(const SParams<C>& S, const float (&xn)[C::XD], float (&w)[C::J]) {
     float c0[C::XD], c1[C::XD], c2[C::XD];
 #pragma unroll
-    for (int d = 0; d < C::XD; ++d) {
-        float sn, cs;
-        sincosf(1.5707963267948966f * xn[d], &sn, &cs);
-        const float cs2 = cs * cs;
-        const float k = S.wsc[d];
-        c0[d] = cs2 * cs2;
-        c1[d] = -4.0f * cs2 * cs * sn * k;
-        c2[d] = (12.0f * cs2 * sn * sn - 4.0f * cs2 * cs2) * k * k;
-    }
+    for (int d = 0; d < C::XD; ++d) window_1d<C>(S, d, xn[d], c0[d], c1[d], c2[d]);
     float prod = 1.f;
 #pragma unroll
     for (int d = 0; d < C::XD; ++d) prod *= c0[d];

@@ -98,7 +98,12 @@ def level_params(il, xd, subdomain_xs, subdomain_ws, unnorm):
     return [xmins, xmaxs, wmins, wmaxs, flags, unnorms, pous]
 
 
-def _static_from_levels(levels, xd):
+WINDOWS = ("cosine", "sigmoid", "bump", "wendland", "rbf")  # fbpinns/windows.py, FBP_WINDOW_* order
+
+
+def _static_from_levels(levels, xd, window="cosine"):
+    if window not in WINDOWS:
+        raise ValueError(f"window must be one of {WINDOWS}, not {window!r}")
     ps = [np.concatenate([lv[k] for lv in levels]) for k in range(7)]
     xmins0 = ps[0] + ps[2] / 2  # centre lines of the overlap regions (scheduler)
     xmaxs0 = ps[1] - ps[3] / 2
@@ -109,6 +114,7 @@ def _static_from_levels(levels, xd):
         "subdomain": {"params": t[:-1], "pou": t[-1]},
         "xmins0": xmins0,
         "xmaxs0": xmaxs0,
+        "window": window,
     }
 
 
@@ -116,9 +122,13 @@ class RectangularDecompositionND(Decomposition):
     """ND hyperrectangular subdomains on a regular grid (fbpinns/decompositions.py:101-335)."""
 
     @staticmethod
-    def init_params(subdomain_xs, subdomain_ws, unnorm):
+    def init_params(subdomain_xs, subdomain_ws, unnorm, window="cosine"):
+        """``window`` (this engine's extension; the reference's decompositions
+        always use the cosine window, decompositions.py:197-199): one of the
+        window functions of fbpinns/windows.py, computed with its derivative
+        jets in the kernels -- "cosine", "sigmoid", "bump", "wendland", "rbf"."""
         xd = len(subdomain_xs)
-        return _static_from_levels([level_params(0, xd, subdomain_xs, subdomain_ws, unnorm)], xd), {}
+        return _static_from_levels([level_params(0, xd, subdomain_xs, subdomain_ws, unnorm)], xd, window), {}
 
     # per-point functions, batched over pairs: params are the gathered per-pair
     # subdomain params (xmins (s,xd), xmaxs, flags (s,1), unnorms (s,2))
@@ -134,8 +144,9 @@ class RectangularDecompositionND(Decomposition):
 
     @staticmethod
     def window_fn(params, x):
-        p = params["static"]["decomposition"]["subdomain"]["params"]
-        return p[4] * windows.cosine(p[0], p[1], x) + (1 - p[4])
+        dec = params["static"]["decomposition"]
+        p = dec["subdomain"]["params"]
+        return p[4] * window_values(dec.get("window", "cosine"), p, x) + (1 - p[4])
 
     @staticmethod
     def inside_points(all_params, x_batch):
@@ -161,14 +172,14 @@ class MultilevelRectangularDecompositionND(RectangularDecompositionND):
     (fbpinns/decompositions.py:338-375)."""
 
     @staticmethod
-    def init_params(subdomain_xss, subdomain_wss, unnorm):
+    def init_params(subdomain_xss, subdomain_wss, unnorm, window="cosine"):
         nms = [tuple(len(x) for x in sx) for sx in subdomain_xss]
         if any(len(nm) != len(nms[0]) for nm in nms):
             raise ValueError("subdomain_xss are not all the same dimensionality")
         xd = len(subdomain_xss[0])
         levels = [level_params(il, xd, sx, sw, unnorm)
                   for il, (sx, sw) in enumerate(zip(subdomain_xss, subdomain_wss))]
-        return _static_from_levels(levels, xd), {}
+        return _static_from_levels(levels, xd, window), {}
 
 
 # ---------------------------------------------------------------------------
@@ -224,6 +235,14 @@ def build_cell_grid(xmins, xmaxs, cells_per_width=4, max_cells=1 << 21):
     np.cumsum(counts, out=start[1:])
     return {"ncell": nc, "lo": lo, "inv_h": inv_h, "cell_start": start.astype(np.int32),
             "cell_boxes": boxes[order].astype(np.int32)}
+
+
+def window_values(name, p, x):
+    """The named window of fbpinns/windows.py for boxes p (the subdomain
+    params [xmins, xmaxs, wmins, wmaxs, ...], broadcastable against x)."""
+    if name == "sigmoid":
+        return windows.sigmoid(p[0], p[1], p[2], p[3], x)
+    return getattr(windows, name)(p[0], p[1], x)
 
 
 def subdomain_arrays(static):

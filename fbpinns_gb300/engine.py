@@ -386,6 +386,7 @@ class FBPINNEngine:
         n.theta = _lib.ptr(self.theta if theta is None else theta)
         n.xmins, n.xmaxs, n.flags, n.unnorms = _lib.ptr(g.xmins), _lib.ptr(g.xmaxs), _lib.ptr(g.flags), _lib.ptr(g.unnorms)
         n.m = self.m
+        n.window, n.wmins, n.wmaxs = g.window, _lib.ptr(g.wmins), _lib.ptr(g.wmaxs)
         return n
 
     def set_problem(self, spec):

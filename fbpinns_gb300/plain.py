@@ -10,11 +10,12 @@ the same masked kernel.  This is what a direct GPU port of the reference step
 (fbpinns/trainers.py:126-177, 213-247, 285-296) looks like in PyTorch.
 """
 
-import math
 
 import numpy as np
 import torch
 
+from . import windows
+from .decompositions import WINDOWS as _WINDOWS
 from .engine import constrained_jets, jet_index
 from .networks import unpack_layers
 
@@ -76,7 +77,11 @@ class PlainStep:
         un = g.unnorms[ids]
         u = u * un[:, None, 1:2] + un[:, None, 0:1]
         flag = g.flags[ids][:, None, None]
-        win = torch.prod(((1 + torch.cos(math.pi * (xg - mu) / sd)) / 2) ** 2, dim=-1, keepdim=True)
+        wname = _WINDOWS[g.window]
+        if wname == "sigmoid":
+            win = windows.sigmoid(lo, hi, g.wmins[ids][:, None, :], g.wmaxs[ids][:, None, :], xg)
+        else:
+            win = getattr(windows, wname)(lo, hi, xg)
         win = flag * win + (1 - flag)
         f = u * win
         xd, d2 = eng.xd, eng.d2mask

@@ -33,6 +33,12 @@ class CellGrid:
         self.flags = flags.to(self.device).contiguous()
         self.unnorms = unnorms.to(self.device).contiguous()
         self.pou = pou.to(self.device).contiguous()
+        # window of the subdomain networks and the overlap widths the sigmoid window reads
+        from .decompositions import WINDOWS
+        self.window = WINDOWS.index(static.get("window", "cosine"))
+        p = static["subdomain"]["params"]
+        self.wmins = p[2].float().to(self.device).contiguous()
+        self.wmaxs = p[3].float().to(self.device).contiguous()
         self.cell_start = torch.as_tensor(g["cell_start"], device=self.device)
         self.cell_boxes = torch.as_tensor(g["cell_boxes"], device=self.device)
         self.ncell, self.lo, self.inv_h = g["ncell"], g["lo"], g["inv_h"]

@@ -70,6 +70,16 @@ extern "C" {
  * gradients of W1 and b1 are written as zero. */
 #define FBP_ACT_FOURIER 4
 
+/* Window of each subdomain network (fbp_net.window), fbpinns/windows.py:
+ * the decompositions use the cosine window (decompositions.py:197-199); the
+ * others are the module's alternatives, each a product over dims of a 1D
+ * window of the box (sigmoid also of its overlap widths wmin, wmax). */
+#define FBP_WINDOW_COSINE 0    /* ((1 + cos(pi (x-mu)/sd)) / 2)^2, windows.py:25-35 */
+#define FBP_WINDOW_SIGMOID 1   /* logistic ramps over wmin / wmax, windows.py:11-22 */
+#define FBP_WINDOW_BUMP 2      /* exp(3 / (((x-mu)/sd)^2 - 1.001)) / exp(-3), windows.py:38-46 */
+#define FBP_WINDOW_WENDLAND 3  /* (1-r)^4 (4r+1), r = |x-mu|/sd, windows.py:49-59 */
+#define FBP_WINDOW_RBF 4       /* exp(-8 ((x-mu)/sd)^2) per dim, windows.py:62-68 */
+
 /* Device status word bits (written by kernels into an int32 the caller owns). */
 #define FBP_STATUS_PAIR_OVERFLOW 1      /* more pairs than the pair capacity */
 #define FBP_STATUS_SLOT_OVERFLOW 2      /* more (point, level) slots than capacity */
@@ -132,6 +142,9 @@ typedef struct fbp_net {
     const float* flags;   /* (m,) window flag (decompositions.py:169-172) */
     const float* unnorms; /* (m, 2) (mu, sd) of the output unnormalisation */
     int64_t m;
+    int32_t window;       /* FBP_WINDOW_* (0: cosine) */
+    const float* wmins;   /* (m, xd) overlap widths below / above the box: */
+    const float* wmaxs;   /* read by FBP_WINDOW_SIGMOID only (nullable otherwise) */
 } fbp_net;
 
 /* Pair lists sorted subdomain-major, and the work queue over them. */

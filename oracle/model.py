@@ -102,6 +102,49 @@ def cosine_window(xmin, xmax, x):
     return torch.prod(ws, dim=1, keepdim=True)
 
 
+def sigmoid_window(xmin, xmax, wmin, wmax, x, tol=1e-8):
+    """``fbpinns/windows.py:11-22`` batched: logistic ramps over the overlaps."""
+    t = math.log((1 - tol) / tol)
+    mu_min, sd_min = xmin + wmin / 2, wmin / (2 * t)
+    mu_max, sd_max = xmax - wmax / 2, wmax / (2 * t)
+    ws = torch.sigmoid((x - mu_min) / sd_min) * torch.sigmoid((mu_max - x) / sd_max)
+    return torch.prod(ws, dim=1, keepdim=True)
+
+
+def bump_window(xmin, xmax, x):
+    """``fbpinns/windows.py:38-46`` batched."""
+    mu, sd = (xmin + xmax) / 2, (xmax - xmin) / 2
+    ws = torch.exp(3 / (((x - mu) / sd) ** 2 - 1.001)) / math.exp(-3)
+    return torch.prod(ws, dim=1, keepdim=True)
+
+
+def wendland_window(xmin, xmax, x):
+    """``fbpinns/windows.py:49-59`` batched."""
+    mu, sd = (xmin + xmax) / 2, (xmax - xmin) / 2
+    r = torch.abs((x - mu) / sd)
+    ws = ((1 - r) ** 4) * (4 * r + 1)
+    ws = heaviside1(x - xmin) * heaviside1(xmax - x) * ws
+    return torch.prod(ws, dim=1, keepdim=True)
+
+
+def rbf_window(xmin, xmax, x):
+    """``fbpinns/windows.py:62-68`` batched."""
+    mu, sd = (xmin + xmax) / 2, (xmax - xmin) / 2
+    return torch.exp(-0.5 * torch.sum(((x - mu) / (0.25 * sd)) ** 2, dim=1, keepdim=True))
+
+
+def window(P, m_take, x_take):
+    """The subdomain window named by P["window"] (default the decompositions'
+    cosine, ``decompositions.py:197-199``) at the pairs' points."""
+    name = P.get("window", "cosine")
+    xmin, xmax = P["xmins"][m_take], P["xmaxs"][m_take]
+    if name == "cosine":
+        return cosine_window(xmin, xmax, x_take)
+    if name == "sigmoid":
+        return sigmoid_window(xmin, xmax, P["wmins"][m_take], P["wmaxs"][m_take], x_take)
+    return {"bump": bump_window, "wendland": wendland_window, "rbf": rbf_window}[name](xmin, xmax, x_take)
+
+
 def fcn(layers, x, activation="tanh"):
     """The reference's networks batched over pairs: W (s,fo,fi), b (s,fo) and the
     layer's activation parameters (s,fo): FCN tanh (``fbpinns/networks.py:61-68``),
@@ -161,7 +204,7 @@ def fbpinn_model(P, x_batch, takes, constraining_fn):
     u = unnorm(un[:, 0:1], un[:, 1:2], u_raw)
     # window_fn  (decompositions.py:197-199)
     flag = P["flags"][m_take]
-    w = flag * cosine_window(xmin, xmax, x_take) + (1 - flag)
+    w = flag * window(P, m_take, x_take) + (1 - flag)
     us, ws = u * w, w
     # POU  (trainers.py:163-170)
     uu = torch.cat([us, ws], dim=1)
@@ -249,8 +292,9 @@ def cut_params(P, ims):
     """The ``cut_all`` / ``cut_active`` slicing of subdomain params (trainers.py:394-408)."""
     ims = torch.as_tensor(np.asarray(ims), dtype=torch.long)
     Q = dict(P)
-    for k in ("xmins", "xmaxs", "flags", "unnorms", "pou"):
-        Q[k] = P[k][ims]
+    for k in ("xmins", "xmaxs", "flags", "unnorms", "pou", "wmins", "wmaxs"):
+        if k in P:
+            Q[k] = P[k][ims]
     Q["layers"] = [tuple(t[ims] for t in layer) for layer in P["layers"]]
     return Q
 

@@ -13,8 +13,13 @@ from fbpinns_gb300.networks import pack_layers
 from oracle import model as OM
 
 
-def decomposition(recipe):
+def decomposition(recipe, window="cosine"):
     """Product static decomposition params for a named recipe (float32 tensors)."""
+    if window != "cosine":
+        st = decomposition(recipe)
+        st = {k: v for k, v in st.items() if not k.startswith("_")}
+        st["window"] = window
+        return st
     if recipe in ("ho", "ho2c", "ho_hardbc"):
         sx = [np.linspace(0, 1, 15)]
         return D.RectangularDecompositionND.init_params(sx, get_subdomain_ws(sx, 2.0), (0., 1.))[0]
@@ -95,7 +100,8 @@ def oracle_params(static, layers64, problem=None):
     p = static["subdomain"]["params"]
     P = {"xmins": p[0].double(), "xmaxs": p[1].double(), "flags": p[4].double(), "unnorms": p[5].double(),
          "pou": static["subdomain"]["pou"].double(), "layers": [tuple(t.double() for t in l) for l in layers64],
-         "problem": problem or {}, "problem_trainable": {}}
+         "problem": problem or {}, "problem_trainable": {}, "wmins": p[2].double(), "wmaxs": p[3].double(),
+         "window": static.get("window", "cosine")}
     return P
 
 

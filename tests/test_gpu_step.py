@@ -758,3 +758,44 @@ def test_scheduled_point_set_vs_oracle(cuda):
     assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (loss, loss_ref.item())
     assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, e
     assert np.all(grad[np.setdiff1d(np.arange(m), a_ims)] == 0)
+
+
+@pytest.mark.parametrize("window", ["cosine", "sigmoid", "bump", "wendland", "rbf"])
+@pytest.mark.parametrize("ls,tc", [([2, 8, 8, 1], False), ([2, 16, 16, 1], True)])
+def test_window_kinds_vs_oracle(cuda, window, ls, tc):
+    """Every window of fbpinns/windows.py in the jet kernels (the
+    decompositions' window option): POU-combined jets (u, u_x, u_y, u_xx +
+    u_yy), the fused Poisson loss and the gradients against the float64
+    oracle, whose windows are pinned on the reference's values; FMA kernels
+    (2-8-8-1) and the tensor-core forward and adjoint (2-16-16-1)."""
+    static = decomposition("multilevel", window=window)
+    m = static["m"]
+    layers32 = [(w.float().double(), b.float().double()) for w, b in random_layers(ls, m, seed=17)]
+    x = _points("poisson", 1500, 31)
+    d2 = 3 | _lib.D2_LAPLACIAN
+    eng = _engine(static, layers32, d2, chunk=256, tensor_cores=tc, tc_adjoint=tc)
+    assert eng.tensor_cores == tc and eng.tc_adjoint == tc
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    eng.set_problem(PR.Poisson2D.fused_spec({"static": {"problem": prob_static}}))
+    ps = eng.points(torch.tensor(x))
+    U = FBPINNJet.apply(eng.theta, eng, ps).double().cpu().numpy()
+    eng.forward_pairs(ps)
+    loss = eng.pou_loss(ps).item()
+    grad = eng.adjoint(ps).cpu().numpy()
+    ps.check_status()
+    P = oracle_params(static, layers32, {"sd": 0.1, "n_freq": 6})
+    assert P["window"] == window
+    p = static["subdomain"]["params"]
+    takes, all_ims, (active, a_ims, f_ims) = OT.get_inputs(x, np.ones(m, dtype=int), p[0].numpy(), p[1].numpy(),
+                                                          static["subdomain"]["pou"].numpy())
+    Pc = OM.cut_params(P, all_ims)
+    req = ((0, ()), (0, (0,)), (0, (1,)), (0, (0, 0)), (0, (1, 1)))
+    ujs = OM.fbpinn_forward(Pc, torch.tensor(x, dtype=torch.float64), takes, lambda P_, xb, u: u, OM.get_jmaps(req))
+    for k in range(3):
+        assert rel_err(U[:, k:k + 1], ujs[k].numpy()) < JET_TOL, (window, k)
+    assert rel_err(U[:, 3:4], (ujs[3] + ujs[4]).numpy()) < JET_TOL, window
+    loss_ref, grads, _ = OM.value_and_grad(P, a_ims, f_ims, [[torch.tensor(x, dtype=torch.float64)]], [takes],
+                                           [OM.get_jmaps(_required("poisson"))], OP.Poisson2D)
+    g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
+    assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (window, loss, loss_ref.item())
+    assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, (window, e)

@@ -366,3 +366,20 @@ def test_six_level_model_and_jets_match_reference():
         ref = g[nm]
         err = np.abs(ujs[1 + k].numpy() - ref).max() / np.abs(ref).max()
         assert err < 2e-6, (nm, err)
+
+
+def test_oracle_windows_match_reference():
+    """The oracle's window functions (all five of fbpinns/windows.py) equal the
+    reference's own values on points inside and outside a box."""
+    g = golden("windows_networks.npz")
+    x = torch.tensor(g["x"])
+    lo, hi = torch.tensor(g["lo"])[None], torch.tensor(g["hi"])[None]
+    wl, wh = torch.tensor(g["wl"])[None], torch.tensor(g["wh"])[None]
+    n = x.shape[0]
+    P = {"xmins": lo.repeat(n, 1), "xmaxs": hi.repeat(n, 1), "wmins": wl.repeat(n, 1), "wmaxs": wh.repeat(n, 1)}
+    m_take = torch.arange(n)
+    for name in ("cosine", "sigmoid", "bump", "wendland", "rbf"):
+        P["window"] = name
+        got = OM.window(P, m_take, x).numpy()
+        np.testing.assert_allclose(got, g[f"win_{name}"], rtol=1e-12, atol=1e-14 if name != "sigmoid" else 1e-300,
+                                   err_msg=name)
