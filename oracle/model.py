@@ -346,6 +346,45 @@ def value_and_grad(P_all, active_ims, fixed_ims, constraints, takess, jmapss, pr
     return loss.detach(), grads, gprob
 
 
+def pinn_model(P, x_batch, constraining_fn):
+    """``fbpinns/trainers.py:120-124,179-195`` (``PINN_model``): one network
+    over the whole domain -- the domain's norm_fn (``domains.py:106-110``),
+    the network, the unnorm of ``decomposition_init_kwargs["unnorm"]``, then
+    the constraining operator.  P: "domain_xmin", "domain_xmax" (xd,),
+    "unnorm" (mu, sd), "layers" [(W (fo,fi), b (fo)), ...]."""
+    lo, hi = P["domain_xmin"], P["domain_xmax"]
+    n = x_batch.shape[0]
+    x_norm = norm((hi + lo) / 2, (hi - lo) / 2, x_batch)
+    layers = [tuple(t.expand((n,) + tuple(t.shape)) for t in layer) for layer in P["layers"]]
+    u_raw = fcn(layers, x_norm, P.get("activation", "tanh"))
+    u = unnorm(P["unnorm"][0], P["unnorm"][1], u_raw)
+    return constraining_fn(P, x_batch, u), u_raw
+
+
+def pinn_value_and_grad(P, constraints, jmapss, problem):
+    """``fbpinns/trainers.py:269-306`` (``PINN_loss`` under ``value_and_grad``):
+    the loss and its gradient with respect to every layer tensor."""
+    leaves = []
+    layers = []
+    for layer in P["layers"]:
+        ts = [t.detach().clone().requires_grad_(True) for t in layer]
+        leaves += ts
+        layers.append(tuple(ts))
+    Q = dict(P, layers=layers)
+    constraints_ = []
+    for jmaps, constraint in zip(jmapss, constraints):
+        def u(xb):
+            return pinn_model(Q, xb, problem.constraining_fn)[0], ()
+        constraints_.append(list(constraint) + get_ujs(constraint[0], jmaps, u))
+    loss = problem.loss_fn(Q, constraints_)
+    g = torch.autograd.grad(loss, leaves)
+    grads, o = [], 0
+    for layer in P["layers"]:
+        grads.append(tuple(g[o:o + len(layer)]))
+        o += len(layer)
+    return loss.detach(), grads
+
+
 def adam_update(params, grads, mu, nu, count, lr, b1=0.9, b2=0.999, eps=1e-8, eps_root=0.0):
     """optax ``adam`` = ``scale_by_adam`` + ``scale(-lr)``, then ``apply_updates``.
 

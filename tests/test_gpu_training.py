@@ -223,3 +223,48 @@ def test_autotuner_searches_launches_and_caches(cuda, tmp_path, monkeypatch):
     ch = first["choice"]
     assert (eng.chunk, eng.forward_chunk, eng.schedule, eng.launch_grid, eng.forward_grid) == \
         (ch["chunk"], ch["forward_chunk"], ch["schedule"], ch["grid"], ch["forward_grid"])
+
+
+def test_pinn_trainer_matches_oracle(cuda):
+    """PINNTrainer (the one-box case of the engine) against the oracle's own
+    restatement of the reference PINN (fbpinns/trainers.py:120-124, 179-195,
+    269-306: domain normalisation, one network, unnormalisation, hard
+    constraint, no window and no partition of unity): the same initial
+    network, points and Adam settings give the same loss at each of the
+    first five steps (1e-5) and the same parameters after them (1e-6 of
+    their scale)."""
+    from fbpinns_gb300.networks import FCN, unpack_layers
+    from fbpinns_gb300.trainers import init_subdomain_networks
+    from oracle import model as OM
+    from oracle import problems as OP
+    c = configs.ho(n_steps=5)
+    c.network_init_kwargs = dict(layer_sizes=[1, 32, 32, 1])
+    c.summary_freq, c.test_freq = 1, 5
+    tr = PINNTrainer(c)
+    tr.train()
+    losses = [h["loss"] for h in tr.history]
+    assert len(losses) == 5
+    # the oracle from the same initial network (init_subdomain_networks with m = 1)
+    _, net = init_subdomain_networks(FCN, c.network_init_kwargs, 1, c.seed)
+    layers = [tuple(t[0].double() for t in layer) for layer in net["layers"]]
+    x = torch.linspace(0, 1, 200, dtype=torch.float64).reshape(-1, 1)
+    P = {"domain_xmin": torch.tensor([0.0], dtype=torch.float64), "domain_xmax": torch.tensor([1.0], dtype=torch.float64),
+         "unnorm": (0.0, 1.0), "layers": layers, "problem": {"sd": 0.1, "mu": 4.0, "k": 6400.0}}
+    jm = [OM.get_jmaps(((0, ()), (0, (0,)), (0, (0, 0))))]
+    mus = [tuple(torch.zeros_like(t) for t in layer) for layer in layers]
+    nus = [tuple(torch.zeros_like(t) for t in layer) for layer in layers]
+    for k in range(5):
+        loss, grads = OM.pinn_value_and_grad(P, [[x]], jm, OP.HarmonicOscillator1DHardBC)
+        assert abs(losses[k] - loss.item()) <= 1e-5 * abs(loss.item()), (k, losses[k], loss.item())
+        new, nm, nn = [], [], []
+        for layer, g, mu, nu in zip(P["layers"], grads, mus, nus):
+            out = [OM.adam_update(t, gt, m1, m2, k, 1e-3) for t, gt, m1, m2 in zip(layer, g, mu, nu)]
+            new.append(tuple(o[0] for o in out))
+            nm.append(tuple(o[1] for o in out))
+            nn.append(tuple(o[2] for o in out))
+        P["layers"], mus, nus = new, nm, nn
+    got = unpack_layers(tr.engine.theta, tr.engine.layer_sizes, tr.engine.extra)
+    for lg, lo in zip(got, P["layers"]):
+        for tg, to in zip(lg, lo):
+            tg = tg[0].double().cpu()
+            assert (tg - to).abs().max().item() <= 1e-6 * max(to.abs().max().item(), 1.0)
