@@ -533,6 +533,7 @@ def run_fused(args, world, rank, local):
                            "slots_per_step": slots, "layers": LAYERS, "jet_components": J,
                            "parallelism": f"replicas x{world}", "chunk": step.ps.chunk,
                            "forward_chunk": step.ps.fwd_chunk, "schedule": eng.schedule,
+                           "forward_schedule": eng.fwd_schedule(),
                            "grid": eng.launch_grid, "forward_grid": eng.forward_grid,
                            "autotuned": getattr(eng, "tuned", None),
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",

@@ -8,14 +8,16 @@ points rather than guessed:
 * the work-item sizes (adjoint pairs per item, forward pairs per item): per-item
   set-up (weights into shared memory, tensor-core B operands, the tile
   pipeline's fill and drain, one gradient partial) against load balance;
-* the schedule: ``dynamic`` (a resident grid whose CTAs take the next item from
-  a device counter), ``static`` (CTA b takes items b, b + grid, ...) or
-  ``per_item`` (one CTA per item);
+* the schedule of each of the two jet launches: ``dynamic`` (a resident grid
+  whose CTAs take the next item from a device counter), ``static`` (CTA b takes
+  items b, b + grid, ...) or ``per_item`` (one CTA per item, so that CTAs
+  retire as they finish and kernels of a higher-priority stream get SMs);
 * the CTA count of the adjoint and of the forward launch (0 = every CTA that
   can be resident, else a multiple of the SM count).
 
-The search is coordinate-wise: the item sizes first (dynamic schedule,
-resident grids), then the schedule, then the two CTA counts; every candidate
+The search is coordinate-wise: the item sizes first (dynamic schedules,
+resident grids), then the adjoint's schedule, the forward's, then the two
+CTA counts; every candidate
 builds the work queues for the points and times forward + POU/loss + adjoint
 with CUDA events -- for a pipelined step with the next step's lists rebuilt
 on the higher-priority side stream at the same time, as in the step itself
@@ -98,6 +100,7 @@ def default_candidates(s, m, sms):
 def _apply(engine, choice):
     engine.chunk, engine.forward_chunk = int(choice["chunk"]), int(choice["forward_chunk"])
     engine.schedule = choice["schedule"]
+    engine.forward_schedule = choice.get("forward_schedule", choice["schedule"])
     engine.launch_grid = int(choice["grid"])
     engine.forward_grid = int(choice["forward_grid"])
     engine.adaptive_items = False
@@ -146,6 +149,7 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
             return engine.tuned
     sms = engine.sm_count
     searched = {"item_sizes": [f"{a}/{f}" for a, f in candidates], "schedule": ["dynamic", "static", "per_item"],
+                "forward_schedule": ["dynamic", "static", "per_item"],
                 "grid": [0, sms, 2 * sms, 3 * sms], "forward_grid": [0, sms, 2 * sms]}
     timings = {}
     ev = lambda: torch.cuda.Event(enable_timing=True)
@@ -153,8 +157,8 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
         side_stream = torch.cuda.Stream(device=engine.device, priority=-1)
 
     def run(choice):
-        tag = f"{choice['chunk']}/{choice['forward_chunk']} {choice['schedule']} g{choice['grid']} " \
-              f"fg{choice['forward_grid']}"
+        tag = f"{choice['chunk']}/{choice['forward_chunk']} {choice['schedule']}/{choice['forward_schedule']} " \
+              f"g{choice['grid']} fg{choice['forward_grid']}"
         if tag in timings:
             return timings[tag]
         _apply(engine, choice)
@@ -173,15 +177,17 @@ def tune_work_items(engine, x, caps=None, candidates=None, reps=3, use_cache=Tru
         timings[tag] = a.elapsed_time(b) / reps
         return timings[tag]
 
-    best = {"chunk": candidates[0][0], "forward_chunk": candidates[0][1], "schedule": "dynamic", "grid": 0,
-            "forward_grid": 0}
+    best = {"chunk": candidates[0][0], "forward_chunk": candidates[0][1], "schedule": "dynamic",
+            "forward_schedule": "dynamic", "grid": 0, "forward_grid": 0}
     best_t = None
     stages = [("size", [dict(chunk=a, forward_chunk=f) for a, f in candidates]),
               ("schedule", [dict(schedule=v) for v in searched["schedule"]]),
+              ("forward_schedule", [dict(forward_schedule=v) for v in searched["forward_schedule"]]),
               ("grid", [dict(grid=v) for v in searched["grid"]]),
               ("forward_grid", [dict(forward_grid=v) for v in searched["forward_grid"]])]
     for name, opts in stages:
-        if name in ("grid", "forward_grid") and best["schedule"] == "per_item":
+        if (name == "grid" and best["schedule"] == "per_item") or \
+                (name == "forward_grid" and best["forward_schedule"] == "per_item"):
             continue  # one CTA per item: the grid is the item count
         for o in opts:
             c = dict(best, **o)

@@ -341,17 +341,17 @@ __device__ __forceinline__ void tanh_jet_adj(const float (&z)[C::J], float tp, f
 
 // Window jet (cosine window of fbpinns/windows.py:25-35 times flag plus 1-flag):
 // per dim c = cos^4(phi), phi = (pi/2) xn; derivatives by the chain rule.
-// The 1D window of dim d at the normalised coordinate xn and its first two
-// derivatives with respect to x (inv_sd = dxn/dx); the window kind is the
-// same for every thread of a launch.
-template <class C>
-__device__ __forceinline__ void window_1d(const SParams<C>& S, int d, float xn, float& c0, float& c1, float& c2) {
-    const float is = S.inv_sd[d];
-    switch (S.window) {
-        case FBP_WINDOW_SIGMOID: {  // A(a) B(b), A = B = logistic, a' = sa1 is, b' = -sb1 is
-            const float a = fmaf(S.sg[d][1], xn, S.sg[d][0]), b = fmaf(-S.sg[d][3], xn, S.sg[d][2]);
+// The 1D windows other than the cosine (sigmoid, bump, wendland, rbf) of dim
+// d at the normalised coordinate xn: value and first two derivatives with
+// respect to x.  Kept out of line so that the cosine path, which every
+// decomposition of the reference uses, stays straight-line code.
+static __device__ __noinline__ float3 window_1d_other(int window, float xn, float is, float4 sg) {
+    float c0, c1, c2;
+    switch (window) {
+        case FBP_WINDOW_SIGMOID: {  // A(a) B(b), A = B = logistic, a = sg.x + sg.y xn, b = sg.z - sg.w xn
+            const float a = fmaf(sg.y, xn, sg.x), b = fmaf(-sg.w, xn, sg.z);
             const float A = 1.0f / (1.0f + __expf(-a)), B = 1.0f / (1.0f + __expf(-b));
-            const float ka = S.sg[d][1] * is, kb = S.sg[d][3] * is;
+            const float ka = sg.y * is, kb = sg.w * is;
             const float A1 = A * (1.0f - A) * ka, A2 = A * (1.0f - A) * (1.0f - 2.0f * A) * ka * ka;
             const float B1 = -B * (1.0f - B) * kb, B2 = B * (1.0f - B) * (1.0f - 2.0f * B) * kb * kb;
             c0 = A * B;
@@ -375,22 +375,33 @@ __device__ __forceinline__ void window_1d(const SParams<C>& S, int d, float xn, 
             c2 = 20.0f * om2 * (4.0f * r - 1.0f) * is * is;
             break;
         }
-        case FBP_WINDOW_RBF: {  // exp(-0.5 (xn / 0.25)^2) = exp(-8 xn^2)
+        default: {  // rbf: exp(-0.5 (xn / 0.25)^2) = exp(-8 xn^2)
             const float g = __expf(-8.0f * xn * xn);
             c0 = g;
             c1 = -16.0f * xn * g * is;
             c2 = (256.0f * xn * xn - 16.0f) * g * is * is;
-            break;
         }
-        default: {  // cosine: cos^4(phi), phi = pi xn / 2
-            float sn, cs;
-            sincosf(1.5707963267948966f * xn, &sn, &cs);
-            const float cs2 = cs * cs;
-            const float k = S.wsc[d];
-            c0 = cs2 * cs2;
-            c1 = -4.0f * cs2 * cs * sn * k;
-            c2 = (12.0f * cs2 * sn * sn - 4.0f * cs2 * cs2) * k * k;
-        }
+    }
+    return make_float3(c0, c1, c2);
+}
+
+// The 1D window of dim d: value and first two derivatives with respect to x.
+template <class C>
+__device__ __forceinline__ void window_1d(const SParams<C>& S, int d, float xn, float& c0, float& c1, float& c2) {
+    if (S.window == FBP_WINDOW_COSINE) {  // cos^4(phi), phi = pi xn / 2
+        float sn, cs;
+        sincosf(1.5707963267948966f * xn, &sn, &cs);
+        const float cs2 = cs * cs;
+        const float k = S.wsc[d];
+        c0 = cs2 * cs2;
+        c1 = -4.0f * cs2 * cs * sn * k;
+        c2 = (12.0f * cs2 * sn * sn - 4.0f * cs2 * cs2) * k * k;
+    } else {
+        const float3 r = window_1d_other(S.window, xn, S.inv_sd[d],
+                                         make_float4(S.sg[d][0], S.sg[d][1], S.sg[d][2], S.sg[d][3]));
+        c0 = r.x;
+        c1 = r.y;
+        c2 = r.z;
     }
 }
 

@@ -392,6 +392,10 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             if (ti > 0 && NBUF == 2)
                 tc_epilogue<C>(S, tmem + (uint32_t)(((ti - 1) % NBUF) * J * 16), warp, act_p, w_p, pos_p, pair_out);
             if (!stage) break;
+            // this tile's window jet (for its epilogue) while its MMAs run
+            window_jet<C>(S, xn, w_p);
+            pos_p = pos;
+            act_p = act;
             // every thread waits; the verdict is made CTA-uniform before the
             // warp-collective tcgen05.ld of the epilogue
             failed = __syncthreads_or(!mbar_wait_bounded(mbar, phase, wait_ns));
@@ -401,9 +405,6 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             }
             phase ^= 1u;
             tc_fence_after();
-            window_jet<C>(S, xn, w_p);
-            pos_p = pos;
-            act_p = act;
             if constexpr (NBUF == 1) {
                 // one TMEM buffer: the epilogue runs before the next tile's MMAs
                 __syncwarp();

@@ -247,7 +247,8 @@ class PointSet:
             p.items, p.n_items = _lib.ptr(self.items_all), _lib.ptr(self.n_items_all)
         p.items_cap = self.items_cap
         p.slots_cap = self.slot_out.shape[0]
-        if self.eng.schedule == "dynamic" and self.dynamic:
+        sched = self.eng.schedule if adjoint else self.eng.fwd_schedule()
+        if sched == "dynamic" and self.dynamic:
             p.item_ctr = _lib.ptr(self.item_ctr[1 if adjoint else 0])
         return p
 
@@ -323,6 +324,9 @@ class FBPINNEngine:
         if schedule not in ("dynamic", "static", "per_item"):
             raise ValueError(f"schedule must be 'dynamic', 'static' or 'per_item', not {schedule!r}")
         self.schedule = schedule
+        # the forward launch's own schedule when set (None: the same as schedule);
+        # set by the autotuner, which searches the two separately
+        self.forward_schedule = None
         # cut the work-item sizes for small pair counts (PointSet._allocate)
         self.adaptive_items = bool(adaptive_items)
         self.sm_count = torch.cuda.get_device_properties(self.device).multi_processor_count
@@ -358,6 +362,9 @@ class FBPINNEngine:
         self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
         self.npou = self.grid.npou
         self._problem = None
+
+    def fwd_schedule(self):
+        return self.schedule if self.forward_schedule is None else self.forward_schedule
 
     # -- parameters ----------------------------------------------------------
     def set_theta(self, theta):
@@ -416,7 +423,7 @@ class FBPINNEngine:
         lib = _lib.load()
         net = self.net_struct(theta)
         pr = ps.pairs_struct(False)
-        grid = ps.forward_items_cap if self.schedule == "per_item" else \
+        grid = ps.forward_items_cap if self.fwd_schedule() == "per_item" else \
             (self.launch_grid if self.forward_grid is None else self.forward_grid)
         if self.tensor_cores:
             _lib.check(lib.fbp_forward_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.pair_out),

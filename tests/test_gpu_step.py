@@ -696,7 +696,7 @@ def test_work_item_autotuner(cuda):
     eng.set_problem(spec)
     cands = [(256, 256), (256, 1024), (512, 2048)]
     tuned = tune_work_items(eng, x, candidates=cands, use_cache=False)
-    sizes = {f"{a}/{f} dynamic g0 fg0": (a, f) for a, f in cands}
+    sizes = {f"{a}/{f} dynamic/dynamic g0 fg0": (a, f) for a, f in cands}
     assert set(sizes) <= set(tuned["timings_ms"])
     best_size = min(sizes, key=lambda k: tuned["timings_ms"][k])
     ch = tuned["choice"]
@@ -710,7 +710,7 @@ def test_work_item_autotuner(cuda):
     loss = eng.pou_loss(ps).item()
     ref = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=best[0], forward_chunk=best[1],
                        adaptive_items=False, schedule=ch["schedule"], grid=ch["grid"])
-    ref.forward_grid = ch["forward_grid"]
+    ref.forward_grid, ref.forward_schedule = ch["forward_grid"], ch["forward_schedule"]
     ref.set_theta(eng.theta.clone())
     ref.set_problem(spec)
     ps2 = ref.points(x)

@@ -218,11 +218,12 @@ def test_autotuner_searches_launches_and_caches(cuda, tmp_path, monkeypatch):
     first, second = out
     assert first["cache"] == "miss" and second["cache"] == "hit"
     assert second["choice"] == first["choice"]
-    assert set(first["searched"]) == {"item_sizes", "schedule", "grid", "forward_grid"}
+    assert set(first["searched"]) == {"item_sizes", "schedule", "forward_schedule", "grid", "forward_grid"}
     assert len(first["timings_ms"]) >= len(first["searched"]["item_sizes"]) + 2
     ch = first["choice"]
     assert (eng.chunk, eng.forward_chunk, eng.schedule, eng.launch_grid, eng.forward_grid) == \
         (ch["chunk"], ch["forward_chunk"], ch["schedule"], ch["grid"], ch["forward_grid"])
+    assert eng.fwd_schedule() == ch["forward_schedule"]
 
 
 def test_pinn_trainer_matches_oracle(cuda):
