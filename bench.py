@@ -450,7 +450,7 @@ def run_fused(args, world, rank, local):
     # DRAM traffic of the adjoint per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
     # adjoint_pairs_kernel<Cfg<2,16,16,11>> in one capture of this workload at 2^16 points
     # (52.60 MB + 0.50 MB for 2,342,187 pairs), scaled by this run's pairs (traffic grows with the pairs)
-    traffic = (52.6016e6 + 0.502528e6) / 2342187 * pairs if (dom == "adjoint_pairs" and J == 4) else None
+    traffic = (52.580352e6 + 0.478976e6) / 2342389 * pairs if (dom == "adjoint_pairs" and J == 4) else None
     roofline = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": best, "unit": "TFLOP/s", "frac": ach / best,
                 "peak_source": "FP32 FMA probe (fbp_fma_probe) measured in this run; MEASURED_PEAKS.json has no FP32 figure",
                 "traffic": traffic,

@@ -85,11 +85,12 @@ def poisson(n_steps=10000, small=False):
                      summary_freq=max(1, n_steps // 10), test_freq=max(1, n_steps // 5))
 
 
-def wave(n_steps=10000, small=False, seed=0):
+def wave(n_steps=10000, small=False, seed=0, min_width=None):
     """(2+1)D wave, c=1: 15x15x4 subdomains (width 2.9x spacing), FCN 3-32-32-1,
-    58^3 grid, 12 seeded Gaussian sources (widths U[0.02, 0.2])."""
+    58^3 grid, 12 seeded Gaussian sources (widths U[min_width, 0.2], min_width
+    0.02 by default)."""
     rng = np.random.default_rng(seed)
-    wlo = 0.1 if small else 0.02
+    wlo = min_width if min_width is not None else (0.1 if small else 0.02)
     src = np.concatenate([rng.uniform(-0.5, 0.5, (12, 2)), rng.uniform(wlo, 0.2, (12, 1)), np.ones((12, 1))], 1)
     sx = [np.linspace(-1, 1, 15), np.linspace(-1, 1, 15), np.linspace(0, 1, 4)]
     g = 20 if small else 58
@@ -139,8 +140,10 @@ def main():
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--layers", default=None, help="network layer sizes, e.g. 1,32,1 (default: the config's)")
     ap.add_argument("--test-every", type=int, default=0, help="steps between test-L1 evaluations (default n/5)")
+    ap.add_argument("--min-width", type=float, default=None, help="wave: lower bound of the source widths")
     a = ap.parse_args()
-    c = CONFIGS[a.config](n_steps=a.steps, small=a.small)
+    kw = {} if a.min_width is None else {"min_width": a.min_width}
+    c = CONFIGS[a.config](n_steps=a.steps, small=a.small, **kw)
     c.engine = a.engine
     if a.layers:
         c.network_init_kwargs = dict(c.network_init_kwargs, layer_sizes=[int(v) for v in a.layers.split(",")])
@@ -152,7 +155,7 @@ def main():
     torch.cuda.synchronize()
     wall = time.time() - t0
     rates = [h["rate"] for h in tr.history[1:]] or [h["rate"] for h in tr.history]
-    print(json.dumps({"config": a.config, "engine": a.engine, "steps": a.steps, "small": a.small,
+    print(json.dumps({"config": a.config, "engine": a.engine, "steps": a.steps, "small": a.small, **kw,
                       "layers": c.network_init_kwargs["layer_sizes"],
                       "test_l1_normalised": [r[2] for r in tr.u_test_losses],
                       "wall_s": round(wall, 2), "steps_per_s": float(np.median(rates)) if rates else None,

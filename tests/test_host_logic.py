@@ -465,6 +465,18 @@ def test_configurations_set_up_on_the_host(name):
     assert np.prod(small.ns[0]) <= np.prod(c.ns[0])
 
 
+def test_wave_source_width_bound():
+    """The wave workload's 12 sources keep their centres (same seed) when the
+    lower bound of their widths changes; the ansatz's hand-over time t1 is the
+    smallest width / c0."""
+    from fbpinns_gb300 import configs
+    a = np.asarray(configs.wave(n_steps=10).problem_init_kwargs["source"])
+    b = np.asarray(configs.wave(n_steps=10, min_width=0.1).problem_init_kwargs["source"])
+    assert a.shape == b.shape == (12, 4)
+    np.testing.assert_array_equal(a[:, :2], b[:, :2])
+    assert 0.02 <= a[:, 2].min() < 0.1 <= b[:, 2].min() and b[:, 2].max() <= 0.2
+
+
 def test_constants_and_model_files_round_trip(tmp_path, monkeypatch):
     """Constants files and model pickles in the reference's layout
     (results/summaries/<run>/constants_<run>.pickle, results/models/<run>/
