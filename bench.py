@@ -40,6 +40,11 @@ LEVELS = [1, 2, 4, 8, 16, 32]
 WIDTH = 2.9
 LR = 1e-3
 SEED = 0
+# DRAM bytes (read + write) of one adjoint launch and the pairs it covered, from an ncu
+# capture of this workload at 2^16 points: layer 2 recomputed, and z-jets read from the
+# forward's store (the forward then writes 256 B per pair more)
+ADJ_DRAM_RECOMPUTE = (52.580352e6 + 0.478976e6, 2342389)
+ADJ_DRAM_STORED = (689.641984e6 + 3.272704e6, 2342389)
 METRIC = "FBPINN train steps/s, fused adjoint vs plain GPU step, at matched test L1 error"
 WORKLOAD = "poisson2d_multilevel_m1365_fcn2-16-16-1_n262144_resampled"
 
@@ -323,7 +328,8 @@ def run_fused(args, world, rank, local):
     d2 = 3 if args.per_dim_jets else 3 | _lib.D2_LAPLACIAN
     tca = args.tc_adjoint
     eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
-                       schedule=args.schedule, forward_chunk=args.forward_chunk, tc_adjoint=tca)
+                       schedule=args.schedule, forward_chunk=args.forward_chunk, tc_adjoint=tca,
+                       store_z2=args.store_z2)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
@@ -363,7 +369,7 @@ def run_fused(args, world, rank, local):
         # the work-item sizes of the resampled step (autotuned there)
         eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
                             tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
-                            tc_adjoint=tca)
+                            tc_adjoint=tca, store_z2=args.store_z2)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -421,6 +427,9 @@ def run_fused(args, world, rank, local):
         eng.tensor_cores = True
     timed("pou_loss", lambda: eng.pou_loss(ps))
     timed("adjoint_pairs", lambda: eng.adjoint(ps, reduce=False))
+    if ps.zs is not None:  # the same two kernels without the stored layer-2 z-jets, for comparison
+        timed("forward_pairs_nostore", lambda: eng.forward_pairs(ps, z2=False))
+        timed("adjoint_pairs_recompute", lambda: eng.adjoint(ps, reduce=False, z2=False))
     if lib.fbp_has_tc_adjoint_shape(2, LAYERS[1], LAYERS[2], d2, _lib.ACT_TANH):
         # the other adjoint variant on the same pairs, for comparison
         eng.tc_adjoint = not eng.tc_adjoint
@@ -448,9 +457,10 @@ def run_fused(args, world, rank, local):
     dom = max(("forward_pairs", "adjoint_pairs"), key=lambda k: timings[k])
     ach = (fl_adj if dom == "adjoint_pairs" else fl_fwd) / (timings[dom] * 1e-3) / 1e12
     # DRAM traffic of the adjoint per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
-    # adjoint_pairs_kernel<Cfg<2,16,16,11>> in one capture of this workload at 2^16 points
-    # (52.60 MB + 0.50 MB for 2,342,187 pairs), scaled by this run's pairs (traffic grows with the pairs)
-    traffic = (52.580352e6 + 0.478976e6) / 2342389 * pairs if (dom == "adjoint_pairs" and J == 4) else None
+    # adjoint_pairs_kernel<Cfg<2,16,16,11>> in one capture of this workload at 2^16 points, scaled
+    # by this run's pairs (traffic grows with the pairs); per variant (bytes, pairs of the capture)
+    adj_dram = ADJ_DRAM_STORED if ps.zs is not None else ADJ_DRAM_RECOMPUTE
+    traffic = adj_dram[0] / adj_dram[1] * pairs if (dom == "adjoint_pairs" and J == 4 and adj_dram) else None
     roofline = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": best, "unit": "TFLOP/s", "frac": ach / best,
                 "peak_source": "FP32 FMA probe (fbp_fma_probe) measured in this run; MEASURED_PEAKS.json has no FP32 figure",
                 "traffic": traffic,
@@ -492,7 +502,7 @@ def run_fused(args, world, rank, local):
             # the fused step (the benchmarked configuration) over the same k_match steps
             eng4 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
                                 tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
-                                tc_adjoint=tca)
+                                tc_adjoint=tca, store_z2=args.store_z2)
             eng4.set_theta(theta0)
             fstep = FusedStep(eng4, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
                               autotune=args.autotune)
@@ -538,10 +548,12 @@ def run_fused(args, world, rank, local):
                            "autotuned": getattr(eng, "tuned", None),
                            "forward_kernel": "tcgen05 3xTF32" if eng.tensor_cores else "fp32 fma",
                            "adjoint_kernel": "tcgen05 3xTF32 layer-2 recompute + fp32 fma" if eng.tc_adjoint
-                           else "fp32 fma",
+                           else ("fp32 fma, layer-2 z-jets stored by the forward" if ps.zs is not None
+                                 else "fp32 fma, layer 2 recomputed"),
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
-                                 ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4) / 1e6)},
+                                 ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4
+                                   + (pairs * J * LAYERS[2] * 4 if ps.zs is not None else 0)) / 1e6)},
                 "e2e": e2e, "gpu_launches": per_step * args.steps, "clocks": clocks, "roofline": roofline,
                 "cpu_baseline": cpu, "plain": plain, "test_l1": l1_fused, "loss_last": loss_last,
                 "evals_per_s": value * pairs}
@@ -624,7 +636,7 @@ def run_extras(args):
         out["networks"][name] = {"layers": ls, "activation": act, "ms_per_step": ms, "steps_per_s": 1000.0 / ms}
         del step, eng
     # inference on a fixed point set (the test step)
-    eng = FBPINNEngine(static, LAYERS, d2mask=0, device=dev)
+    eng = FBPINNEngine(static, LAYERS, d2mask=0, device=dev, store_z2=False)
     eng.set_theta(init_theta(m))
     g = torch.Generator(device="cpu").manual_seed(SEED)
     xt = torch.rand((N_POINTS, 2), generator=g).to(dev)
@@ -681,6 +693,9 @@ def main():
     ap.add_argument("--fma-forward", action="store_true", help="forward jets on the CUDA-core FMA kernel")
     ap.add_argument("--tc-adjoint", action="store_true",
                     help="adjoint with the layer-2 recompute on the tensor cores (fbp_adjoint_pairs_tc)")
+    ap.add_argument("--store-z2", action="store_const", const=True, default=None,
+                    help="the forward stores the layer-2 z-jets and the adjoint reads them instead of recomputing "
+                         "(default: only for hidden layers at least 32 wide, so not for this workload)")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

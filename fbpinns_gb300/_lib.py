@@ -64,7 +64,7 @@ class Net(C.Structure):
 class Pairs(C.Structure):
     _fields_ = [("sd_start", C.c_void_p), ("sd_rec", C.c_void_p),
                 ("items", C.c_void_p), ("n_items", C.c_void_p), ("items_cap", C.c_int64), ("slots_cap", C.c_int64),
-                ("item_ctr", C.c_void_p)]
+                ("item_ctr", C.c_void_p), ("zs", C.c_void_p), ("zs_cap", C.c_int64)]
 
 
 class Problem(C.Structure):

@@ -141,10 +141,13 @@ def main():
     ap.add_argument("--layers", default=None, help="network layer sizes, e.g. 1,32,1 (default: the config's)")
     ap.add_argument("--test-every", type=int, default=0, help="steps between test-L1 evaluations (default n/5)")
     ap.add_argument("--min-width", type=float, default=None, help="wave: lower bound of the source widths")
+    ap.add_argument("--z2", default="auto", choices=["auto", "store", "recompute"],
+                    help="layer-2 z-jets for the adjoint: stored by the forward or recomputed (auto: by width)")
     a = ap.parse_args()
     kw = {} if a.min_width is None else {"min_width": a.min_width}
     c = CONFIGS[a.config](n_steps=a.steps, small=a.small, **kw)
     c.engine = a.engine
+    c.store_z2 = {"auto": None, "store": True, "recompute": False}[a.z2]
     if a.layers:
         c.network_init_kwargs = dict(c.network_init_kwargs, layer_sizes=[int(v) for v in a.layers.split(",")])
     if a.test_every:
@@ -156,6 +159,7 @@ def main():
     wall = time.time() - t0
     rates = [h["rate"] for h in tr.history[1:]] or [h["rate"] for h in tr.history]
     print(json.dumps({"config": a.config, "engine": a.engine, "steps": a.steps, "small": a.small, **kw,
+                      "z2": a.z2,
                       "layers": c.network_init_kwargs["layer_sizes"],
                       "test_l1_normalised": [r[2] for r in tr.u_test_losses],
                       "wall_s": round(wall, 2), "steps_per_s": float(np.median(rates)) if rates else None,

@@ -107,6 +107,7 @@ class Constants(ConstantsBase):
         self.launch_grid = 0           # CTAs of the persistent jet kernels (0 = 4 per SM)
         self.use_graph = True          # capture the step in a CUDA graph
         self.tensor_cores = None       # forward jets on tcgen05 (3xTF32): None = where compiled, True, False
+        self.store_z2 = None           # forward stores the layer-2 z-jets for the adjoint: None = hidden >= 32
         self.pair_headroom = 1.25      # pair-buffer capacity factor for resampled steps
         self.device_schedule = True    # fused step: follow scheduler changes on the device (no re-capture)
         self.save_models = False       # write model pickles at model_save_freq

@@ -528,11 +528,32 @@ __device__ __forceinline__ void l2_chunk(const SParams<C>& S, const float* a1row
         }
 }
 
+// Stored layer-2 pre-activation jets (fbp_pairs.zs): component-major, one
+// float per (component c, neuron k) row of zs_cap sorted pairs, so that the
+// lanes of a warp (consecutive pairs) touch consecutive words.  zs points at
+// the pair's column; the rows are written once and read once, with streaming
+// (evict-first) accesses.
+template <class C>
+__device__ __forceinline__ void store_z2(float* __restrict__ zs, int64_t zs_cap, int k0, const float (&acc)[C::KC][C::J]) {
+#pragma unroll
+    for (int c = 0; c < C::J; ++c)
+#pragma unroll
+        for (int k = 0; k < C::KC; ++k) __stcs(zs + (size_t)(c * C::H2 + k0 + k) * zs_cap, acc[k][c]);
+}
+template <class C>
+__device__ __forceinline__ void load_z2(const float* __restrict__ zs, int64_t zs_cap, int k0, float (&acc)[C::KC][C::J]) {
+#pragma unroll
+    for (int c = 0; c < C::J; ++c)
+#pragma unroll
+        for (int k = 0; k < C::KC; ++k) acc[k][c] = __ldcs(zs + (size_t)(c * C::H2 + k0 + k) * zs_cap);
+}
+
 // Network output jet (before unnormalisation) for one pair; a1row/stride is the
-// thread's shared-memory slot for its first-layer activations.
+// thread's shared-memory slot for its first-layer activations.  With zs set
+// (networks with two hidden layers) the layer-2 z-jets are stored there.
 template <class C>
 __device__ __forceinline__ void net_jet(const SParams<C>& S, const float (&xn)[C::XD], float* a1row, int stride,
-                                        float (&out)[C::J]) {
+                                        float (&out)[C::J], float* __restrict__ zs = nullptr, int64_t zs_cap = 0) {
 #pragma unroll 4
     for (int n = 0; n < C::H1; ++n) a1row[n * stride] = l1_act<C>(S, xn, n);
 #pragma unroll
@@ -543,6 +564,7 @@ __device__ __forceinline__ void net_jet(const SParams<C>& S, const float (&xn)[C
         for (int ch = 0; ch < C::NCH; ++ch) {
             float acc[C::KC][C::J];
             l2_chunk<C>(S, a1row, stride, ch * C::KC, acc);
+            if (zs) store_z2<C>(zs, zs_cap, ch * C::KC, acc);
 #pragma unroll
             for (int k = 0; k < C::KC; ++k) {
                 const int kk = ch * C::KC + k;
@@ -607,7 +629,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 3) forward_pairs_kernel(fbp_net n
                 for (int d = 0; d < XD; ++d) xr_n[d] = x[(size_t)pt * XD + d];
             }
             float o[J];
-            net_jet<C>(S, xn, &a1s[threadIdx.x], FWD_THREADS, o);
+            net_jet<C>(S, xn, &a1s[threadIdx.x], FWD_THREADS, o, pr.zs ? pr.zs + beg + t : nullptr, pr.zs_cap);
             // unnormalisation (decompositions.py:191-194): u = u_raw*sd + mu
             float u[J];
 #pragma unroll
@@ -821,7 +843,10 @@ __global__ void __launch_bounds__(AdjW<C>::T) adjoint_pairs_kernel(fbp_net net, 
                     if constexpr (C::TWO) {
                         float* zrow = &R.zb[lane * A::ZS];
                         float acc[C::KC][J];
-                        l2_chunk<C>(S, a1row, 1, ch * C::KC, acc);
+                        if (pr.zs)  // stored by the forward of the same lists
+                            load_z2<C>(pr.zs + beg + t0 + lane, pr.zs_cap, ch * C::KC, acc);
+                        else
+                            l2_chunk<C>(S, a1row, 1, ch * C::KC, acc);
 #pragma unroll
                         for (int k = 0; k < C::KC; ++k) {
                             const int kk = ch * C::KC + k;

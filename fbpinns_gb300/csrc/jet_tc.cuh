@@ -170,7 +170,8 @@ __device__ __forceinline__ void tanh_jet_pair(const float2 (&z)[C::J], float2 (&
 // unnormalisation, window product -> the pair's record.
 template <class C>
 __device__ __forceinline__ void tc_epilogue(const SParams<C>& S, uint32_t taddr, int warp, bool act,
-                                            const float (&w)[C::J], int pos, float* __restrict__ pair_out) {
+                                            const float (&w)[C::J], int pos, float* __restrict__ pair_out,
+                                            float* __restrict__ zs, int64_t zs_cap) {
     constexpr int J = C::J, RS = rec_stride(C::J), H2 = 16;
     float acc[J][16];
 #pragma unroll
@@ -189,6 +190,13 @@ __device__ __forceinline__ void tc_epilogue(const SParams<C>& S, uint32_t taddr,
 #pragma unroll
         for (int c = 0; c < J; ++c) z[c] = make_float2(acc[c][k], acc[c][k + 1]);
         z[0] = add2(z[0], *reinterpret_cast<const float2*>(&S.b2[k]));
+        if (zs) {  // the layer-2 z-jets for the adjoint (fbp_pairs.zs: rows c * 16 + k)
+#pragma unroll
+            for (int c = 0; c < J; ++c) {
+                __stcs(zs + (size_t)(c * H2 + k) * zs_cap, z[c].x);
+                __stcs(zs + (size_t)(c * H2 + k + 1) * zs_cap, z[c].y);
+            }
+        }
         if constexpr (C::ACT == FBP_ACT_TANH || C::ACT == FBP_ACT_FOURIER) {
             tanh_jet_pair<C>(z, g);  // layer 2 is a plain tanh
         } else {
@@ -390,7 +398,8 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             }
             __syncwarp();  // the epilogue's tcgen05.ld is warp-collective
             if (ti > 0 && NBUF == 2)
-                tc_epilogue<C>(S, tmem + (uint32_t)(((ti - 1) % NBUF) * J * 16), warp, act_p, w_p, pos_p, pair_out);
+                tc_epilogue<C>(S, tmem + (uint32_t)(((ti - 1) % NBUF) * J * 16), warp, act_p, w_p, pos_p, pair_out,
+                               pr.zs ? pr.zs + beg + (ti - 1) * TC_TILE + tid : nullptr, pr.zs_cap);
             if (!stage) break;
             // this tile's window jet (for its epilogue) while its MMAs run
             window_jet<C>(S, xn, w_p);
@@ -408,7 +417,8 @@ __global__ void __launch_bounds__(TC_TILE) forward_pairs_tc_kernel(fbp_net net, 
             if constexpr (NBUF == 1) {
                 // one TMEM buffer: the epilogue runs before the next tile's MMAs
                 __syncwarp();
-                tc_epilogue<C>(S, tmem, warp, act_p, w_p, pos_p, pair_out);
+                tc_epilogue<C>(S, tmem, warp, act_p, w_p, pos_p, pair_out,
+                               pr.zs ? pr.zs + beg + ti * TC_TILE + tid : nullptr, pr.zs_cap);
                 tc_fence_before();
                 __syncthreads();
                 tc_fence_after();

@@ -181,6 +181,11 @@ class PointSet:
         self.slot_out = torch.empty((max(u_cap, 1), R), dtype=torch.float32, device=dev)
         self.grad_part = torch.empty((self.items_cap, eng.P), dtype=torch.float32, device=dev)
         self.U = torch.empty((self.n, self.J), dtype=torch.float32, device=dev)
+        # layer-2 z-jets of every sorted pair, written by the forward and read by
+        # the adjoint of a training step (fbp_pairs.zs): J * h2 rows of s_cap
+        self.zs = None
+        if eng.z2_rows and eng.z2_rows * max(s_cap, 1) * 4 <= eng.z2_limit:
+            self.zs = torch.empty((eng.z2_rows, max(s_cap, 1)), dtype=torch.float32, device=dev)
         self._sized = True
 
     def rebuild(self, stream=None, state=None):
@@ -238,7 +243,10 @@ class PointSet:
                                       _lib.ptr(self.n_items_act), self.items_cap, _lib.ptr(t_status(self)),
                                       _lib.ptr(self.work_scratch), ws, st), "fbp_build_work")
 
-    def pairs_struct(self, adjoint=False):
+    def pairs_struct(self, adjoint=False, z2=True):
+        """The launch's fbp_pairs; z2: pass the stored layer-2 z-jets buffer
+        (when this point set has one) -- only for a forward and the adjoint
+        that follows it with the same parameters."""
         p = _lib.Pairs()
         p.sd_start, p.sd_rec = _lib.ptr(self.sd_start), _lib.ptr(self.sd_rec)
         if adjoint:
@@ -250,6 +258,8 @@ class PointSet:
         sched = self.eng.schedule if adjoint else self.eng.fwd_schedule()
         if sched == "dynamic" and self.dynamic:
             p.item_ctr = _lib.ptr(self.item_ctr[1 if adjoint else 0])
+        if z2 and self.zs is not None:
+            p.zs, p.zs_cap = _lib.ptr(self.zs), self.zs.shape[1]
         return p
 
     def subdomain_counts(self):
@@ -275,7 +285,8 @@ class FBPINNEngine:
     """Packed parameters + kernel launches for one decomposition and network shape."""
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
-                 activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True, tc_adjoint=None):
+                 activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True, tc_adjoint=None,
+                 store_z2=None):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -346,6 +357,18 @@ class FBPINNEngine:
             raise _lib.FBPLibraryError(f"no tensor-core adjoint kernel for layer sizes {ls} ({activation}, "
                                        f"d2mask {self.d2mask}); compiled: xd-16-16-1 tanh networks")
         self.tc_adjoint = bool(tc_adjoint) and tca_ok
+        # store_z2: the forward of a training step stores the layer-2 z-jets of
+        # every pair (J * h2 floats) and the FMA adjoint reads them instead of
+        # recomputing layer 2 (h1 multiply-adds per stored value); a point set
+        # keeps the buffer while it takes at most z2_limit bytes (an eighth of
+        # the device memory), else the adjoint recomputes.  None: where the first
+        # hidden layer is at least 32 wide (measured: 3-32-32-1 gains, 2-16-16-1
+        # loses -- its stores cost the forward more than the reads save in the
+        # latency-bound adjoint)
+        if store_z2 is None:
+            store_z2 = self.h1 >= 32
+        self.z2_rows = self.J * self.h2 if (store_z2 and self.h2 > 0 and not self.tc_adjoint) else 0
+        self.z2_limit = torch.cuda.get_device_properties(self.device).total_memory // 8
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
         self.m1 = torch.zeros_like(self.theta)
@@ -419,10 +442,12 @@ class FBPINNEngine:
     def points(self, x, select=None, caps=None, chunk=None, scheduled=False):
         return PointSet(self, x, select=select, caps=caps, chunk=chunk, scheduled=scheduled)
 
-    def forward_pairs(self, ps, theta=None, stream=None):
+    def forward_pairs(self, ps, theta=None, stream=None, z2=True):
+        """Per-pair jets into ps.pair_out; z2: also store the layer-2 z-jets
+        for an adjoint that follows (False for jets that are not differentiated)."""
         lib = _lib.load()
         net = self.net_struct(theta)
-        pr = ps.pairs_struct(False)
+        pr = ps.pairs_struct(False, z2)
         grid = ps.forward_items_cap if self.fwd_schedule() == "per_item" else \
             (self.launch_grid if self.forward_grid is None else self.forward_grid)
         if self.tensor_cores:
@@ -469,11 +494,14 @@ class FBPINNEngine:
                    "fbp_loss_finalize")
         return self.loss
 
-    def adjoint(self, ps, theta=None, out=None, stream=None, reduce=True):
+    def adjoint(self, ps, theta=None, out=None, stream=None, reduce=True, z2=True):
+        """Gradient partials of the loss seeds in ps.slot_out; z2: read the
+        layer-2 z-jets stored by the forward_pairs(..., z2=True) that preceded
+        it with the same parameters (False: recompute them)."""
         lib = _lib.load()
         st = _lib.stream_ptr(stream)
         net = self.net_struct(theta)
-        pr = ps.pairs_struct(True)
+        pr = ps.pairs_struct(True, z2)
         grid = ps.items_cap if self.schedule == "per_item" else self.launch_grid
         if self.tc_adjoint:
             _lib.check(lib.fbp_adjoint_pairs_tc(C.byref(net), _lib.ptr(ps.x), C.byref(pr), _lib.ptr(ps.slot_out),
@@ -530,7 +558,8 @@ class FBPINNJet(torch.autograd.Function):
     @staticmethod
     def forward(ctx, theta, engine, ps):
         theta = theta.contiguous()
-        engine.forward_pairs(ps, theta)
+        # autograd may run other forwards on ps before this backward: no stored z-jets
+        engine.forward_pairs(ps, theta, z2=False)
         U = engine.pou_forward(ps).clone()
         ctx.engine, ctx.ps = engine, ps
         ctx.save_for_backward(theta)
@@ -542,7 +571,7 @@ class FBPINNJet(torch.autograd.Function):
         eng, ps = ctx.engine, ctx.ps
         eng.pou_backward(ps, Ubar)
         grad = torch.empty_like(theta)
-        eng.adjoint(ps, theta, out=grad)
+        eng.adjoint(ps, theta, out=grad, z2=False)
         return grad, None, None
 
 

@@ -430,7 +430,7 @@ class FBPINNTrainer:
                 d2 = d2g
         eng = FBPINNEngine(st_dec, layer_sizes, d2, device=dev, chunk=c.chunk, grid=c.launch_grid,
                            tensor_cores=getattr(c, "tensor_cores", None), activation=activation,
-                           forward_chunk=getattr(c, "forward_chunk", None))
+                           forward_chunk=getattr(c, "forward_chunk", None), store_z2=getattr(c, "store_z2", None))
         eng.set_theta(pack_layers(eng_layers))
         for k, v in list(all_params["trainable"].get("problem", {}).items()):
             all_params["trainable"]["problem"][k] = torch.as_tensor(v, dtype=torch.float32).to(dev).clone()
@@ -604,7 +604,7 @@ class FBPINNTrainer:
             setattr(eng, key, (x, ps))
         ps = getattr(eng, key)[1]
         with torch.no_grad():
-            eng.forward_pairs(ps)
+            eng.forward_pairs(ps, z2=False)
             U = eng.pou_forward(ps)
             return problem.constraining_fn(all_params, x, U[:, 0:1])
 

@@ -163,6 +163,15 @@ typedef struct fbp_pairs {
      * other streams take fewer.  The results do not depend on the schedule.
      * Concurrent launches need distinct counters. */
     int32_t* item_ctr;
+    /* Optional (NULL: the adjoint recomputes them): the layer-2
+     * pre-activation jets of every sorted pair, float32, component-major
+     * ((c * h2 + k) * zs_cap + sorted pair index; zs_cap >= the pair count).
+     * fbp_forward_pairs and fbp_forward_pairs_tc write them for networks with
+     * two hidden layers; fbp_adjoint_pairs then reads them instead of
+     * recomputing layer 2.  The adjoint must follow a forward of the same
+     * lists and parameters with the same buffer. */
+    float* zs;
+    int64_t zs_cap;
 } fbp_pairs;
 
 /* Built-in PDE residuals fused into the POU/loss kernel. */

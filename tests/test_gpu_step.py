@@ -799,3 +799,52 @@ def test_window_kinds_vs_oracle(cuda, window, ls, tc):
     g_ref = torch.cat([t.reshape(len(a_ims), -1) for dw, db in grads for t in (dw, db)], 1).numpy()
     assert abs(loss - loss_ref.item()) <= JET_TOL * abs(loss_ref.item()), (window, loss, loss_ref.item())
     assert (e := rel_err(grad[a_ims], g_ref)) < GRAD_TOL, (window, e)
+
+
+@pytest.mark.parametrize("name,lap,tc,act", [("poisson_bench", True, True, "tanh"), ("poisson_bench", True, False, "tanh"),
+                                             ("poisson_bench", False, True, "tanh"),
+                                             ("poisson_bench", False, False, "tanh"),
+                                             ("wave_bench", True, False, "tanh"), ("poisson", True, False, "adaptive_tanh"),
+                                             ("poisson", False, False, "sin")])
+def test_stored_layer2_jets_match_recompute(cuda, name, lap, tc, act):
+    """The adjoint reading the layer-2 z-jets stored by the forward
+    (fbp_pairs.zs) against the same adjoint recomputing them: bitwise equal
+    gradients after the FMA forward (the same sums in the same order), within
+    1e-6 after the tensor-core forward (3xTF32 z-jets); a point set over the
+    memory limit keeps no buffer and recomputes."""
+    recipe, ls, pcls, pkw, ocls, opar, d2 = CASES[name]
+    static = decomposition(recipe)
+    scale = 1.0 if act in ("tanh", "adaptive_tanh") else math.sqrt(6.0)
+    gen = torch.Generator().manual_seed(71)
+    layers = [(w * scale, b * scale) + tuple(0.5 + torch.rand(b.shape, generator=gen, dtype=torch.float64)
+                                             for _ in range(_lib.ACT_EXTRA[act]))
+              for w, b in random_layers(ls, static["m"], seed=5)]
+    theta = pack_layers([tuple(t.float() for t in layer) for layer in layers])
+    x = _points(recipe if recipe != "multilevel" else "poisson", 2000, 23)
+    prob_static = pcls.init_params(**pkw)[0]
+    d2e = d2 | (0 if not lap else _lib.D2_LAPLACIAN if d2 == 3 else _lib.D2_GROUP(3))
+
+    def run(limit=None):
+        eng = FBPINNEngine(static, ls, d2e, chunk=1024, activation=act, tensor_cores=tc, store_z2=True)
+        if limit is not None:
+            eng.z2_limit = limit
+        eng.set_theta(theta)
+        eng.set_problem(pcls.fused_spec({"static": {"problem": prob_static}}))
+        ps = eng.points(torch.tensor(x))
+        eng.forward_pairs(ps)
+        loss = eng.pou_loss(ps).item()
+        g_store = eng.adjoint(ps).clone()
+        g_recompute = eng.adjoint(ps, z2=False).clone()
+        ps.check_status()
+        return eng, ps, loss, g_store, g_recompute
+
+    eng, ps, loss, gs, gr = run()
+    assert ps.zs is not None and tuple(ps.zs.shape) == (eng.J * ls[2], ps.s_cap)
+    assert eng.tensor_cores == tc
+    if tc:
+        assert (e := rel_err(gs.cpu().numpy(), gr.cpu().numpy())) < 1e-6, e
+    else:
+        assert torch.equal(gs, gr)
+    _, ps0, loss0, gs0, gr0 = run(limit=0)
+    assert ps0.zs is None and loss0 == loss
+    assert torch.equal(gs0, gr0) and torch.equal(gr0, gr)
