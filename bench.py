@@ -329,7 +329,7 @@ def run_fused(args, world, rank, local):
     tca = args.tc_adjoint
     eng = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid, tensor_cores=tc,
                        schedule=args.schedule, forward_chunk=args.forward_chunk, tc_adjoint=tca,
-                       store_z2=args.store_z2)
+                       store_z2=args.store_z2, cell_order=args.cell_order)
     eng.set_theta(theta0)
     npts = args.points
     step = FusedStep(eng, spec, opt, resample=(npts, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
@@ -369,7 +369,7 @@ def run_fused(args, world, rank, local):
         # the work-item sizes of the resampled step (autotuned there)
         eng2 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
                             tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
-                            tc_adjoint=tca, store_z2=args.store_z2)
+                            tc_adjoint=tca, store_z2=args.store_z2, cell_order=args.cell_order)
         eng2.set_theta(theta0)
         rng = np.random.default_rng(seed + 7)
         nh = 4
@@ -480,7 +480,7 @@ def run_fused(args, world, rank, local):
     u_exact = problem.exact_solution(all_params, x_test).to(dev)
     if not args.no_plain:
         try:
-            eng3 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk)
+            eng3 = FBPINNEngine(static, LAYERS, d2mask=3, device=dev, chunk=args.chunk, cell_order=args.cell_order)
             eng3.set_theta(theta0)
             pstep = PlainStep(eng3, problem, all_params, ((0, (0, 0)), (0, (1, 1))), opt,
                               resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed))
@@ -502,7 +502,7 @@ def run_fused(args, world, rank, local):
             # the fused step (the benchmarked configuration) over the same k_match steps
             eng4 = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, chunk=args.chunk, grid=args.grid,
                                 tensor_cores=tc, schedule=args.schedule, forward_chunk=args.forward_chunk,
-                                tc_adjoint=tca, store_z2=args.store_z2)
+                                tc_adjoint=tca, store_z2=args.store_z2, cell_order=args.cell_order)
             eng4.set_theta(theta0)
             fstep = FusedStep(eng4, spec, opt, resample=(N_POINTS, [0.0, 0.0], [1.0, 1.0], seed), use_graph=True,
                               autotune=args.autotune)
@@ -551,6 +551,7 @@ def run_fused(args, world, rank, local):
                            else ("fp32 fma, layer-2 z-jets stored by the forward" if ps.zs is not None
                                  else "fp32 fma, layer 2 recomputed"),
                            "jet": "u, grad u, u_xx, u_yy" if args.per_dim_jets else "u, grad u, laplacian u",
+                           "point_order": "morton cells of ~64 points" if eng.cell_order else "as drawn",
                            "l2": "per-step working set ~%.0f MB > 129 MB L2; no flush" %
                                  ((pairs * (2 * J * 4 + 16) + slots * 2 * J * 4
                                    + (pairs * J * LAYERS[2] * 4 if ps.zs is not None else 0)) / 1e6)},
@@ -696,6 +697,8 @@ def main():
     ap.add_argument("--store-z2", action="store_const", const=True, default=None,
                     help="the forward stores the layer-2 z-jets and the adjoint reads them instead of recomputing "
                          "(default: only for hidden layers at least 32 wide, so not for this workload)")
+    ap.add_argument("--no-cell-order", dest="cell_order", action="store_false",
+                    help="keep each drawn batch in the sampler's order (default: Morton cell order)")
     ap.add_argument("--per-dim-jets", action="store_true",
                     help="carry u_xx and u_yy as separate jet components instead of the Laplacian")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

@@ -107,6 +107,9 @@ _SIG = {
                            _P, _P]),
     "fbp_sample_uniform": (C.c_int, [_P, _I64, _I32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64,
                                      C.c_uint64, _P, _P]),
+    "fbp_sort_points_scratch_bytes": (C.c_size_t, [_I64, _I32]),
+    "fbp_sort_points_cells": (C.c_int, [_P, _I64, _I32, C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P,
+                                        C.c_size_t, _P]),
     "fbp_graph_instantiate": (C.c_int, [_P, _I32, C.POINTER(C.c_void_p)]),
     "fbp_graph_launch": (C.c_int, [_P, _P]),
     "fbp_graph_exec_destroy": (C.c_int, [_P]),

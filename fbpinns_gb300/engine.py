@@ -286,7 +286,7 @@ class FBPINNEngine:
 
     def __init__(self, static_decomp, layer_sizes, d2mask, device="cuda", chunk=1024, grid=None, tensor_cores=None,
                  activation="tanh", schedule="dynamic", forward_chunk=None, adaptive_items=True, tc_adjoint=None,
-                 store_z2=None):
+                 store_z2=None, cell_order=True):
         if not torch.cuda.is_available():
             raise _lib.FBPLibraryError("the FBPINN engine needs a CUDA device (no CPU fallback)")
         _lib.load()
@@ -369,6 +369,13 @@ class FBPINNEngine:
             store_z2 = self.h1 >= 32
         self.z2_rows = self.J * self.h2 if (store_z2 and self.h2 > 0 and not self.tc_adjoint) else 0
         self.z2_limit = torch.cuda.get_device_properties(self.device).total_memory // 8
+        # sample(): uniform batches in the order of a Morton cell grid (locality of
+        # the lists and jets; the same points, so the same batch)
+        self.cell_order = bool(cell_order)
+        self._order_bufs = {}
+        # the decomposition's bounding box: the cell grid of batches given by the caller
+        self.extent = (self.grid.xmins.min(0).values.double().cpu().tolist(),
+                       self.grid.xmaxs.max(0).values.double().cpu().tolist())
         dev = self.device
         self.theta = torch.zeros((self.m, self.P), dtype=torch.float32, device=dev)
         self.m1 = torch.zeros_like(self.theta)
@@ -537,13 +544,46 @@ class FBPINNEngine:
         self.adam(lr, stream=stream, **adam_kw)
         return loss
 
-    def sample(self, x_out, seed, offset, xmin, xmax, counter=None, stream=None):
-        """Uniform points into x_out; the stream offset is offset + *counter."""
+    def sample(self, x_out, seed, offset, xmin, xmax, counter=None, stream=None, order=None):
+        """Uniform points into x_out; the stream offset is offset + *counter.
+        order (None: the engine's cell_order): the drawn batch in the order of
+        the Morton cells of [xmin, xmax] (fbp_sort_points_cells), the same
+        points for the same seed and offset."""
         lib = _lib.load()
         lo = (C.c_double * 3)(*[float(v) for v in xmin])
         hi = (C.c_double * 3)(*[float(v) for v in xmax])
-        _lib.check(lib.fbp_sample_uniform(_lib.ptr(x_out), x_out.shape[0], self.xd, lo, hi, int(seed), int(offset),
+        n = int(x_out.shape[0])
+        order = (self.cell_order if order is None else bool(order)) and n > 0
+        dst = self._order_buffers(n)[0] if order else x_out
+        _lib.check(lib.fbp_sample_uniform(_lib.ptr(dst), n, self.xd, lo, hi, int(seed), int(offset),
                                           _lib.ptr(counter), _lib.stream_ptr(stream)), "fbp_sample_uniform")
+        if order:
+            self.order_points(dst, x_out, stream, (xmin, xmax))
+
+    def _order_buffers(self, n):
+        """(drawn batch, sort scratch) for batches of n points, kept per size:
+        the resampled and host-point steps order one batch at a time, on one stream."""
+        buf = self._order_bufs.get(n)
+        if buf is None:
+            nb = int(_lib.load().fbp_sort_points_scratch_bytes(n, self.xd))
+            buf = (torch.empty((n, self.xd), dtype=torch.float32, device=self.device),
+                   torch.empty(nb // 4 + 1, dtype=torch.int32, device=self.device))
+            self._order_bufs[n] = buf
+        return buf
+
+    def order_points(self, x_in, x_out, stream=None, box=None):
+        """x_out = the points x_in in Morton cell order over box (default: the
+        decomposition's bounding box), fbp_sort_points_cells."""
+        lib = _lib.load()
+        n = int(x_in.shape[0])
+        if n == 0:
+            return
+        xmin, xmax = self.extent if box is None else box
+        lo = (C.c_double * 3)(*[float(v) for v in xmin])
+        hi = (C.c_double * 3)(*[float(v) for v in xmax])
+        scratch = self._order_buffers(n)[1]
+        _lib.check(lib.fbp_sort_points_cells(_lib.ptr(x_in), n, self.xd, lo, hi, _lib.ptr(x_out), _lib.ptr(scratch),
+                                             scratch.numel() * 4, _lib.stream_ptr(stream)), "fbp_sort_points_cells")
 
 
 class FBPINNJet(torch.autograd.Function):

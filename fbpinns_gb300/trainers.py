@@ -208,8 +208,19 @@ class FusedStep:
         if pipeline is None:
             pipeline = resample is not None
         self.pipeline = bool(pipeline) and (resample is not None or self.host)
+        # host batches land in a staging buffer and enter the point set in Morton
+        # cell order (engine.cell_order: the same batch, in an order with locality)
+        self.order_host = self.host and engine.cell_order
+        if self.order_host:
+            self.ps.x_stage = torch.empty_like(self.ps.x)
+            # the cell grid spans the probe batch (later batches: the same distribution)
+            lo, hi = x0.min(0).values.double(), x0.max(0).values.double()
+            pad = 1e-6 * torch.clamp(hi - lo, min=1.0)
+            self.order_box = ((lo - pad).cpu().tolist(), (hi + pad).cpu().tolist())
         if self.pipeline:
             self.sets = [self.ps, engine.points(self.ps.x.clone(), caps=caps, scheduled=self.scheduled)]
+            if self.order_host:
+                self.sets[1].x_stage = torch.empty_like(self.ps.x)
             self.cur = 0
             self.started = False
             self.snap = torch.zeros(1, dtype=torch.int32, device=dev)  # count at the step's start
@@ -258,6 +269,8 @@ class FusedStep:
             self.side.wait_stream(main)
             if self.resample is not None:
                 eng.sample(b.x, self.seed, 1, self.xmin, self.xmax, counter=self.snap, stream=self.side)
+            elif self.order_host:
+                eng.order_points(b.x_stage, b.x, stream=self.side, box=self.order_box)
             b.rebuild(stream=self.side)
         loss = eng.fused_step(a, o["learning_rate"], stream=main, b1=o["b1"], b2=o["b2"], eps=o["eps"],
                               eps_root=o["eps_root"])
@@ -270,6 +283,8 @@ class FusedStep:
             eng.sample(self.ps.x, self.seed, 0, self.xmin, self.xmax, counter=eng.count, stream=stream)
             self.ps.rebuild(stream=stream)
         elif self.host:
+            if self.order_host:
+                eng.order_points(self.ps.x_stage, self.ps.x, stream=stream, box=self.order_box)
             self.ps.rebuild(stream=stream)
         return eng.fused_step(self.ps, o["learning_rate"], stream=stream, b1=o["b1"], b2=o["b2"], eps=o["eps"],
                               eps_root=o["eps_root"])
@@ -322,12 +337,18 @@ class FusedStep:
             if x_next is None:
                 raise ValueError("a pipelined host-point step needs the next step's points (x_next)")
             if not self.started:
-                self.sets[self.cur].x.copy_(x_host, non_blocking=True)
-                self.sets[self.cur].rebuild()
+                cur = self.sets[self.cur]
+                if self.order_host:
+                    cur.x_stage.copy_(x_host, non_blocking=True)
+                    self.eng.order_points(cur.x_stage, cur.x, box=self.order_box)
+                else:
+                    cur.x.copy_(x_host, non_blocking=True)
+                cur.rebuild()
                 self.started = True
-            self.sets[1 - self.cur].x.copy_(x_next, non_blocking=True)
+            nxt = self.sets[1 - self.cur]
+            (nxt.x_stage if self.order_host else nxt.x).copy_(x_next, non_blocking=True)
         elif self.host:
-            self.ps.x.copy_(x_host, non_blocking=True)
+            (self.ps.x_stage if self.order_host else self.ps.x).copy_(x_host, non_blocking=True)
         if self.pipeline:
             if self.use_graph:
                 if self.graph is None:

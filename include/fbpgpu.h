@@ -422,6 +422,21 @@ int fbp_adam(float* theta, float* m1, float* m2, const float* grad, const uint8_
 int fbp_sample_uniform(float* x, int64_t n, int32_t xd, const double* xmin, const double* xmax,
                        uint64_t seed, uint64_t offset, const int32_t* counter, void* stream);
 
+/* Scratch bytes of fbp_sort_points_cells for n points of dimension xd. */
+size_t fbp_sort_points_scratch_bytes(int64_t n, int32_t xd);
+
+/* x_out (n, xd) = the points x_in in the order of the Morton index of a
+ * regular grid of cells over [xmin, xmax] (about 64 points per cell, at most
+ * 2^16 cells), points of one cell in their input order: a stable counting
+ * sort, so the result depends on the input only.  The reference's uniform
+ * batches (fbpinns/domains.py:113-142) are i.i.d. and enter the loss as a mean,
+ * so the ordered batch is the same batch; the order keeps points that share
+ * subdomains together for the interaction lists and the jet kernels.  x_in and
+ * x_out must not overlap.  Asynchronous on stream; no host synchronisation. */
+int fbp_sort_points_cells(const float* x_in, int64_t n, int32_t xd, const double* xmin, const double* xmax,
+                          float* x_out, void* scratch, size_t scratch_bytes, void* stream);
+
+
 /* Executable graph of a captured training step (cudaGraph_t graph) whose
  * kernel nodes keep the priority of the stream they were captured from
  * (graph instantiated with cudaGraphInstantiateFlagUseNodePriority), so
