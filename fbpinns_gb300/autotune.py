@@ -50,13 +50,14 @@ def cache_path():
 def config_key(engine, n, pipelined):
     """The configuration a tuned launch is valid for: the GPU, the network and
     its jet, the kernels used (and whether layer 2 is stored for the adjoint),
-    the subdomain and point counts and whether the
+    whether batches are put in cell order, the subdomain and point counts and whether the
     next step's lists are built alongside (a redrawn batch of the same size
     keeps the key; its pair count is recorded with the choice)."""
     props = torch.cuda.get_device_properties(engine.device)
     return "|".join(str(v) for v in (props.name, props.multi_processor_count, engine.layer_sizes, engine.activation,
                                      engine.d2mask, int(engine.tensor_cores), int(getattr(engine, "tc_adjoint", 0)),
-                                     int(bool(getattr(engine, "z2_rows", 0))), engine.m, int(n), int(bool(pipelined))))
+                                     int(bool(getattr(engine, "z2_rows", 0))), int(bool(getattr(engine, "cell_order", 0))),
+                                     engine.m, int(n), int(bool(pipelined))))
 
 
 def _load_cache(path):
