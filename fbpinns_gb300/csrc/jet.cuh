@@ -390,7 +390,7 @@ template <class C>
 __device__ __forceinline__ void window_1d(const SParams<C>& S, int d, float xn, float& c0, float& c1, float& c2) {
     if (S.window == FBP_WINDOW_COSINE) {  // cos^4(phi), phi = pi xn / 2
         float sn, cs;
-        sincosf(1.5707963267948966f * xn, &sn, &cs);
+        sincospif(0.5f * xn, &sn, &cs);  // sin, cos of pi (xn / 2): no general range reduction
         const float cs2 = cs * cs;
         const float k = S.wsc[d];
         c0 = cs2 * cs2;
