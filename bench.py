@@ -532,9 +532,31 @@ def run_fused(args, world, rank, local):
         t_cpu, nsteps, _ = cpu_steps(ref, N_POINTS, 30, 1, budget_s=10.0)
         cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": threads, "kind": "port",
                "sample": f"{nsteps} full steps of the workload ({N_POINTS} points, {ref.pairs} pairs); " + CPU_KIND}
+        # the GPU step against the restatement at the full size: loss and gradient of the
+        # initial parameters on one batch of the workload, computed by both
+        try:
+            xb = np.random.default_rng(SEED + 7).uniform(0, 1, (N_POINTS, 2)).astype(np.float32)
+            loss_c, grad_c = cpu_reference_step(static, theta0.cpu(), threads).loss_grad(xb)
+            engp = FBPINNEngine(static, LAYERS, d2mask=d2, device=dev, tensor_cores=tc, cell_order=False)
+            engp.set_theta(theta0)
+            engp.set_problem(spec)
+            psp = engp.points(torch.from_numpy(xb).to(dev))
+            engp.forward_pairs(psp)
+            loss_g = float(engp.pou_loss(psp).item())
+            grad_g = engp.adjoint(psp).cpu().numpy()
+            psp.check_status()
+            cpu["agreement"] = {"points": N_POINTS, "pairs": int(psp.s), "loss_gpu": loss_g, "loss_cpu": loss_c,
+                                "loss_rel_diff": abs(loss_g - loss_c) / abs(loss_c),
+                                "grad_max_abs_diff_over_max_abs": float(np.abs(grad_g - grad_c).max()
+                                                                        / np.abs(grad_c).max()),
+                                "against": "the C restatement above (FP32 arithmetic, FP64 loss sum) on the "
+                                           "initial parameters and one batch; the FP64 oracle is the tests' pin"}
+            del engp, psp
+        except Exception as ex:  # reported, not hidden
+            cpu["agreement"] = {"error": repr(ex)[:200]}
 
     # launches of our kernels in one step (counted from the C-ABI calls of the step body)
-    per_step = (1 + 1 + 3 + 3 + 1 + 6 + 5 + 5 + 1 + 1 + 1 + 1 + 1 + 2)
+    per_step = (1 + 1 + 3 + 3 + 1 + 6 + 5 + 5 + 1 + 1 + 1 + 1 + 1 + 2) + (4 if eng.cell_order else 0)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
