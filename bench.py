@@ -43,7 +43,7 @@ SEED = 0
 # DRAM bytes (read + write) of one adjoint launch and the pairs it covered, from an ncu
 # capture of this workload at 2^16 points: layer 2 recomputed, and z-jets read from the
 # forward's store (the forward then writes 256 B per pair more)
-ADJ_DRAM_RECOMPUTE = (52.580352e6 + 0.478976e6, 2342389)
+ADJ_DRAM_RECOMPUTE = (52.580352e6 + 0.155392e6, 2342389)
 ADJ_DRAM_STORED = (689.641984e6 + 3.272704e6, 2342389)
 METRIC = "FBPINN train steps/s, fused adjoint vs plain GPU step, at matched test L1 error"
 WORKLOAD = "poisson2d_multilevel_m1365_fcn2-16-16-1_n262144_resampled"
