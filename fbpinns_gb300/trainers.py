@@ -212,9 +212,15 @@ class FusedStep:
         # cell order (engine.cell_order: the same batch, in an order with locality)
         self.order_host = self.host and engine.cell_order
         if self.order_host:
-            self.ps.x_stage = torch.empty_like(self.ps.x)
-            # the cell grid spans the probe batch (later batches: the same distribution)
+            # the cell grid spans the probe batch (later batches: the same
+            # distribution; points outside it gather in its edge cells, which
+            # stays correct but slows the ordering); no order for a probe
+            # with non-finite coordinates or no extent along a dim
             lo, hi = x0.min(0).values.double(), x0.max(0).values.double()
+            ok = bool(torch.isfinite(lo).all() and torch.isfinite(hi).all() and (hi > lo).all())
+            self.order_host = ok
+        if self.order_host:
+            self.ps.x_stage = torch.empty_like(self.ps.x)
             pad = 1e-6 * torch.clamp(hi - lo, min=1.0)
             self.order_box = ((lo - pad).cpu().tolist(), (hi + pad).cpu().tolist())
         if self.pipeline:

@@ -431,8 +431,11 @@ size_t fbp_sort_points_scratch_bytes(int64_t n, int32_t xd);
  * sort, so the result depends on the input only.  The reference's uniform
  * batches (fbpinns/domains.py:113-142) are i.i.d. and enter the loss as a mean,
  * so the ordered batch is the same batch; the order keeps points that share
- * subdomains together for the interaction lists and the jet kernels.  x_in and
- * x_out must not overlap.  Asynchronous on stream; no host synchronisation. */
+ * subdomains together for the interaction lists and the jet kernels.  A cell
+ * of L points is ordered in O(L^2) work (one warp per cell), so batches
+ * concentrated in a few cells of the box order correctly but slowly.  x_in
+ * and x_out must not overlap.  Asynchronous on stream; no host
+ * synchronisation. */
 int fbp_sort_points_cells(const float* x_in, int64_t n, int32_t xd, const double* xmin, const double* xmax,
                           float* x_out, void* scratch, size_t scratch_bytes, void* stream);
 
