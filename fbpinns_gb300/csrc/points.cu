@@ -55,10 +55,13 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
 __device__ __forceinline__ uint32_t cell_of(const float* __restrict__ x, int64_t i, const CellGrid& g) {
     const int top = (1 << g.bits) - 1;
     uint32_t c[3] = {0u, 0u, 0u};
-    for (int d = 0; d < g.xd; ++d) {
-        const float f = (x[i * g.xd + d] - g.lo[d]) * g.scale[d];
-        int v = f >= 0.f ? (int)f : 0;  // NaN and negatives to cell 0
-        c[d] = (uint32_t)(v > top ? top : v);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {  // unrolled over the largest xd: c stays in registers
+        if (d < g.xd) {
+            const float f = (x[i * g.xd + d] - g.lo[d]) * g.scale[d];
+            int v = f >= 0.f ? (int)f : 0;  // NaN and negatives to cell 0
+            c[d] = (uint32_t)(v > top ? top : v);
+        }
     }
     if (g.xd == 1) return c[0];
     if (g.xd == 2) return spread2(c[0]) | (spread2(c[1]) << 1);
