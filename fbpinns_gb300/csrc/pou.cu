@@ -513,6 +513,9 @@ __device__ __forceinline__ float point_residual(const fbp_problem& P, float inv_
 // seeds dL/dN, and the slot records [dL/dN | W] leave coalesced.  A warp whose
 // slots do not fit the table runs the same steps one point per lane.
 constexpr int POU_WARPS = 4;
+#ifndef POU_ROWS
+#define POU_ROWS 2  // rows scanned together (measured: 2 beats 1)
+#endif
 
 // slots per warp in the shared-memory table: up to 256, within 40 KB per CTA
 __host__ __device__ constexpr int pou_slotcap(int rs) {
@@ -557,61 +560,80 @@ __global__ void __launch_bounds__(POU_WARPS * 32) pou_loss_kernel(fbp_problem P,
             for (int i = lane; i < nsl * RS; i += 32) T[i] = 0.f;
             __syncwarp();
             int prev = -1;  // last slot id of the previous row
-            // row loads, one row ahead of the scan
-            int nkey;
-            float nv[NV];
-            auto load_row = [&](int64_t eb) {
+            // rows of 32 pairs, POU_ROWS at a time (their scans interleave), loaded
+            // one group ahead; lanes past the range hold the key INT_MAX and zeros
+            auto load_row = [&](int64_t eb, int& key, float (&vv)[NV]) {
                 const int64_t e = eb + lane;
-                nkey = e < E1 ? p_take[e] : 0x7fffffff;
+                key = e < E1 ? p_take[e] : 0x7fffffff;
 #pragma unroll
-                for (int c = 0; c < NV; ++c) nv[c] = 0.f;
+                for (int c = 0; c < NV; ++c) vv[c] = 0.f;
                 if (e < E1) {
                     const float4* po = reinterpret_cast<const float4*>(pair_out + (size_t)e * RS);
 #pragma unroll
                     for (int h = 0; h < RS / 4; ++h) {
                         const float4 q = po[h];
-                        if (4 * h + 0 < NV) nv[4 * h + 0] = q.x;
-                        if (4 * h + 1 < NV) nv[4 * h + 1] = q.y;
-                        if (4 * h + 2 < NV) nv[4 * h + 2] = q.z;
-                        if (4 * h + 3 < NV) nv[4 * h + 3] = q.w;
+                        if (4 * h + 0 < NV) vv[4 * h + 0] = q.x;
+                        if (4 * h + 1 < NV) vv[4 * h + 1] = q.y;
+                        if (4 * h + 2 < NV) vv[4 * h + 2] = q.z;
+                        if (4 * h + 3 < NV) vv[4 * h + 3] = q.w;
                     }
                 }
             };
-            if (E0 < E1) load_row(E0);
-            for (int64_t eb = E0; eb < E1; eb += 32) {
-                const int64_t e = eb + lane;
-                const bool ev = e < E1;
-                const int key = nkey;
-                float v[NV];
+            constexpr int ROWS = POU_ROWS;
+            int nkey[ROWS];
+            float nv[ROWS][NV];
 #pragma unroll
-                for (int c = 0; c < NV; ++c) v[c] = nv[c];
-                if (eb + 32 < E1) load_row(eb + 32);
+            for (int r = 0; r < ROWS; ++r) load_row(E0 + 32 * r, nkey[r], nv[r]);
+            for (int64_t eb = E0; eb < E1; eb += 32 * ROWS) {
+                int key[ROWS];
+                float v[ROWS][NV];
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    key[r] = nkey[r];
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) v[r][c] = nv[r][c];
+                }
+                if (eb + 32 * ROWS < E1) {
+#pragma unroll
+                    for (int r = 0; r < ROWS; ++r) load_row(eb + 32 * (ROWS + r), nkey[r], nv[r]);
+                }
                 // slots must ascend along the range (levels ascending within a point)
-                const int kp = __shfl_up_sync(0xffffffffu, key, 1);
-                if (ev && key < (lane ? kp : prev)) atomicOr(status, FBP_STATUS_LEVEL_ORDER);
-                prev = __shfl_sync(0xffffffffu, key, 31);
-                // inclusive scan of the records within runs of equal slot ids
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int kp = __shfl_up_sync(0xffffffffu, key[r], 1);
+                    if (eb + 32 * r + lane < E1 && key[r] < (lane ? kp : prev))
+                        atomicOr(status, FBP_STATUS_LEVEL_ORDER);
+                    prev = __shfl_sync(0xffffffffu, key[r], 31);
+                }
+                // inclusive scans of the records within runs of equal slot ids
 #pragma unroll
                 for (int off = 1; off < 32; off <<= 1) {
-                    const int k2 = __shfl_up_sync(0xffffffffu, key, off);
-                    const bool same = lane >= off && k2 == key;
 #pragma unroll
-                    for (int c = 0; c < NV; ++c) {
-                        const float t = __shfl_up_sync(0xffffffffu, v[c], off);
-                        if (same) v[c] += t;
+                    for (int r = 0; r < ROWS; ++r) {
+                        const int k2 = __shfl_up_sync(0xffffffffu, key[r], off);
+                        const bool same = lane >= off && k2 == key[r];
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) {
+                            const float t = __shfl_up_sync(0xffffffffu, v[r][c], off);
+                            if (same) v[r][c] += t;
+                        }
                     }
                 }
-                const int kn = __shfl_down_sync(0xffffffffu, key, 1);
-                if (ev && (lane == 31 || kn != key)) {  // the run's last lane adds the run's sum
-                    const int s = key - (int)U0;
-                    if (s >= 0 && s < nsl) {
+                // each run's last lane adds the run's sum, row after row
 #pragma unroll
-                        for (int c = 0; c < NV; ++c) T[s * RS + c] += v[c];
-                    } else {
-                        atomicOr(status, FBP_STATUS_BAD_INDEX);
+                for (int r = 0; r < ROWS; ++r) {
+                    const int kn = __shfl_down_sync(0xffffffffu, key[r], 1);
+                    if (eb + 32 * r + lane < E1 && (lane == 31 || kn != key[r])) {
+                        const int s = key[r] - (int)U0;
+                        if (s >= 0 && s < nsl) {
+#pragma unroll
+                            for (int c = 0; c < NV; ++c) T[s * RS + c] += v[r][c];
+                        } else {
+                            atomicOr(status, FBP_STATUS_BAD_INDEX);
+                        }
                     }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
             // per slot: U_l = N / W (quotient-rule jets) in place of N
             for (int s = lane; s < nsl; s += 32) {
