@@ -555,8 +555,12 @@ def run_fused(args, world, rank, local):
         except Exception as ex:  # reported, not hidden
             cpu["agreement"] = {"error": repr(ex)[:200]}
 
-    # launches of our kernels in one step (counted from the C-ABI calls of the step body)
-    per_step = (1 + 1 + 3 + 3 + 1 + 6 + 5 + 5 + 1 + 1 + 1 + 1 + 1 + 2) + (4 if eng.cell_order else 0)
+    # launches of our kernels in one step (counted from the C-ABI calls of the step body; each
+    # scan of up to 4096 tiles of 2048 is two launches, all of them at this size): sample (1),
+    # cell order (4), inside count (1), pair and slot offsets (2 + 2), fill (1), subdomain sort
+    # (hist 1, scan 2, scatter 1, starts 1), two work queues (count 1, scan 2, fill 1 each),
+    # forward, POU/loss, loss finalize, adjoint, gradient reduce, Adam + step count (1+1+1+1+1+2)
+    per_step = 1 + (4 if eng.cell_order else 0) + 1 + 4 + 1 + 5 + 2 * 4 + 7
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",

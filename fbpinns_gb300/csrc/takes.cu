@@ -272,11 +272,27 @@ __global__ void scan_sums_kernel(int32_t* __restrict__ sums, int64_t nb) {
     if (threadIdx.x == 0) sums[nb] = carry;
 }
 
+// Tiles up to which a down-sweep block adds the earlier tiles' sums itself
+// (no scan of the sums in between: two launches per scan instead of three;
+// the loads grow with the square of the tile count).
+constexpr int64_t SCAN_FUSED_TILES = 4096;
+
+// fused: the block's offset is the sum of sums[0 .. blockIdx.x) (tile totals,
+// added here) and the last block writes the total; else sums holds the
+// scanned offsets and the total at sums[nb].
 __global__ void scan_down_kernel(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ sums,
-                                 int64_t nb, int32_t* __restrict__ out) {
+                                 int64_t nb, int32_t* __restrict__ out, bool fused) {
     __shared__ int sw[33];
     __shared__ int tile[SCAN_TILE];
     const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int prefix = 0;
+    if (fused) {
+        int a = 0;
+        for (int64_t i = threadIdx.x; i < (int64_t)blockIdx.x; i += blockDim.x) a += sums[i];
+        block_exclusive_scan(a, sw, prefix);  // prefix = the block total of a
+    } else {
+        prefix = sums[blockIdx.x];
+    }
     // blocked arrangement: thread t owns items [t*V, t*V+V) of the tile
 #pragma unroll
     for (int v = 0; v < SCAN_V; ++v) {
@@ -293,7 +309,7 @@ __global__ void scan_down_kernel(const int32_t* __restrict__ in, int64_t n, cons
     }
     int tot;
     const int ex = block_exclusive_scan(s, sw, tot);
-    const int off = sums[blockIdx.x] + ex;
+    const int off = prefix + ex;
 #pragma unroll
     for (int v = 0; v < SCAN_V; ++v) tile[threadIdx.x * SCAN_V + v] = off + loc[v];
     __syncthreads();
@@ -302,7 +318,10 @@ __global__ void scan_down_kernel(const int32_t* __restrict__ in, int64_t n, cons
         const int64_t i = base + (int64_t)v * SCAN_T + threadIdx.x;
         if (i < n) out[i] = tile[v * SCAN_T + threadIdx.x];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[nb];
+    if (threadIdx.x == 0) {
+        if (fused && blockIdx.x == nb - 1) out[n] = prefix + tot;
+        if (!fused && blockIdx.x == 0) out[n] = sums[nb];
+    }
 }
 
 int scan_launch(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, cudaStream_t st) {
@@ -311,11 +330,14 @@ int scan_launch(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, cudaS
         FBP_CUDA_CHECK(cudaMemsetAsync(out, 0, sizeof(int32_t), st));
         return FBP_OK;
     }
+    const bool fused = nb <= SCAN_FUSED_TILES;
     scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums);
     FBP_LAUNCH_CHECK();
-    scan_sums_kernel<<<1, 1024, 0, st>>>(sums, nb);
-    FBP_LAUNCH_CHECK();
-    scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums, nb, out);
+    if (!fused) {
+        scan_sums_kernel<<<1, 1024, 0, st>>>(sums, nb);
+        FBP_LAUNCH_CHECK();
+    }
+    scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums, nb, out, fused);
     FBP_LAUNCH_CHECK();
     return FBP_OK;
 }

@@ -176,3 +176,22 @@ def test_full_size_poisson_takes(cuda):
     u, inv = np.unique(key, return_inverse=True)
     np.testing.assert_array_equal(_np(takes[2]), inv)
     np.testing.assert_array_equal(_np(takes[3]), u // 64)
+
+
+@pytest.mark.parametrize("n", [1, 2047, 2048, 2049, 5_000_000, 9_000_000])
+def test_exclusive_scan_matches_cumsum(cuda, n):
+    """fbp_scan_i32 against numpy: out[i] = sum in[:i], out[n] = the total --
+    up to 4096 tiles of 2048 (the down-sweep adds the earlier tiles' sums
+    itself) and beyond (a scan of the tile sums in between)."""
+    from fbpinns_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(n)
+    x = rng.integers(0, 200, n).astype(np.int32)
+    xin = torch.from_numpy(x).cuda()
+    out = torch.full((n + 1,), -1, dtype=torch.int32, device="cuda")
+    nb = int(lib.fbp_scan_scratch_bytes(n))
+    scratch = torch.empty(nb // 4 + 1, dtype=torch.int32, device="cuda")
+    _lib.check(lib.fbp_scan_i32(_lib.ptr(xin), _lib.ptr(out), n, _lib.ptr(scratch), nb, _lib.stream_ptr()),
+               "fbp_scan_i32")
+    ref = np.concatenate([[0], np.cumsum(x, dtype=np.int64)]).astype(np.int32)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
