@@ -376,13 +376,18 @@ __global__ void compact_kernel(const int32_t* __restrict__ flag, const int32_t* 
 // its chunk in order and scatters with ranks from __match_any_sync, keeping
 // per-bucket running counts in shared memory: stable and deterministic.
 // ---------------------------------------------------------------------------
-#ifndef FBP_SORT_CH
-// pairs per chunk of the subdomain sort: each chunk costs O(m) in tables and
-// histogram entries besides its pairs (measured with cell-ordered batches:
-// 4096 0.382 ms, 8192 0.364, 16384 0.33, 32768 0.32 for the whole list build)
-#define FBP_SORT_CH 16384
-#endif
-constexpr int SORT_CH = FBP_SORT_CH;
+// Pairs per chunk of the subdomain sort, from the pair capacity: each chunk
+// costs O(m) in bucket tables and histogram entries besides its pairs, so
+// larger chunks pay while there are enough of them to fill the GPU (about
+// four per SM of a GB300; measured with cell-ordered batches of 9.4e6 pairs:
+// 4096 0.382 ms, 8192 0.364, 16384 0.33 for the whole list build; 2.3e6 pairs:
+// 4096 33.6 us, 16384 55.4 us for the scatter).  A function of s_cap only, so
+// that the scratch size and the launches agree; the order does not depend on it.
+static int64_t sort_chunk(int64_t s_cap) {
+    int64_t ch = 4096;
+    while (ch < 16384 && s_cap / (2 * ch) >= 4 * kSM) ch *= 2;
+    return ch;
+}
 
 // With pt_keep, a pair whose point has pt_keep[point] == 0 is left out (its
 // key reads as -1, outside every bucket); the kept pairs keep their order.
@@ -394,13 +399,14 @@ __device__ __forceinline__ int kept_key(const int32_t* __restrict__ key, const i
 
 __global__ void sort_hist_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
                                  const uint8_t* __restrict__ pt_keep, const int32_t* __restrict__ s_dev,
-                                 int64_t s_cap, int64_t m, int64_t nchunks, int32_t* __restrict__ hist) {
+                                 int64_t s_cap, int64_t m, int64_t nchunks, int64_t chn,
+                                 int32_t* __restrict__ hist) {
     extern __shared__ int cnt[];
     const int64_t s = min((int64_t)*s_dev, s_cap);
     for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         for (int64_t j = threadIdx.x; j < m; j += blockDim.x) cnt[j] = 0;
         __syncthreads();
-        const int64_t b0 = ch * SORT_CH, b1 = min(b0 + SORT_CH, s);
+        const int64_t b0 = ch * chn, b1 = min(b0 + chn, s);
         for (int64_t i0 = b0; i0 < b1; i0 += (int64_t)blockDim.x * 8) {  // loads first, then the counts
             int kk[8];
 #pragma unroll
@@ -424,7 +430,7 @@ constexpr int SCATTER_U = 16;  // 32-pair rows whose loads are issued together
 #endif
 constexpr int SCATTER_W = FBP_SCATTER_W;  // warps per chunk (fewer when their bucket tables do not fit)
 
-// One CTA of W <= SCATTER_W warps per chunk of SORT_CH pairs (point-major).
+// One CTA of W <= SCATTER_W warps per chunk of chn pairs (point-major).
 // Each warp first counts the buckets of its part of the chunk; the running
 // offsets of warp w start at the chunk's bucket offset plus the counts of
 // warps < w, so the warps then place their quarters independently and the
@@ -436,16 +442,16 @@ __global__ void __launch_bounds__(SCATTER_W * 32)
     sort_scatter_kernel(const int32_t* __restrict__ key, const int32_t* __restrict__ n_take,
                         const int32_t* __restrict__ p_take, const uint8_t* __restrict__ pt_keep,
                         const int32_t* __restrict__ s_dev, int64_t s_cap, int64_t m, int64_t nchunks,
-                        const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
+                        int64_t chn, const int32_t* __restrict__ hoff, int4* __restrict__ sd_rec) {
     extern __shared__ int run[];  // [W][m]: per-warp counts, then running offsets
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
     int* myrun = run + (int64_t)w * m;
     const int64_t s = min((int64_t)*s_dev, s_cap);
-    const int64_t SUB = (SORT_CH + W - 1) / W;
+    const int64_t SUB = (chn + W - 1) / W;
     for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         for (int64_t j = threadIdx.x; j < m * W; j += blockDim.x) run[j] = 0;
         __syncthreads();
-        const int64_t c0 = ch * SORT_CH, c1 = min(c0 + SORT_CH, s);
+        const int64_t c0 = ch * chn, c1 = min(c0 + chn, s);
         const int64_t b0 = min(c0 + (int64_t)w * SUB, c1), b1 = min(b0 + SUB, c1);
         for (int64_t i0 = b0; i0 < b1; i0 += 32 * 8) {  // loads of 8 rows first, then the counts
             int kk[8];
@@ -714,7 +720,8 @@ extern "C" int fbp_compact_flags(const int32_t* flag, int64_t n, int32_t* out, i
 }
 
 extern "C" size_t fbp_sort_scratch_bytes(int64_t s_cap, int64_t m) {
-    const int64_t nch = (s_cap + SORT_CH - 1) / SORT_CH;
+    const int64_t chn = sort_chunk(s_cap);
+    const int64_t nch = (s_cap + chn - 1) / chn;
     const int64_t hn = m * nch + 1;
     return (size_t)hn * sizeof(int32_t) * 2 + scan_scratch(hn) + 256;
 }
@@ -731,7 +738,8 @@ static int sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_
     FBP_REQUIRE(scratch && scratch_bytes >= fbp_sort_scratch_bytes(s_cap, m), FBP_ERR_CAPACITY,
                 "fbp_sort_pairs: scratch too small");
     cudaStream_t st = as_stream(stream);
-    const int64_t nch = (s_cap + SORT_CH - 1) / SORT_CH;
+    const int64_t chn = sort_chunk(s_cap);
+    const int64_t nch = (s_cap + chn - 1) / chn;
     const int64_t hn = m * nch;
     int32_t* hist = (int32_t*)scratch;
     int32_t* hoff = hist + (hn + 1);
@@ -746,7 +754,7 @@ static int sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_
             cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(shm * sw)));
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 8);
-        sort_hist_kernel<<<g, 256, shm, st>>>(m_take, n_take, pt_keep, s_dev, s_cap, m, nch, hist);
+        sort_hist_kernel<<<g, 256, shm, st>>>(m_take, n_take, pt_keep, s_dev, s_cap, m, nch, chn, hist);
         FBP_LAUNCH_CHECK();
     }
     int rc = scan_launch(hist, hoff, hn, sums, st);
@@ -754,7 +762,7 @@ static int sort_pairs(const int32_t* m_take, const int32_t* n_take, const int32_
     if (nch > 0) {
         const int g = (int)std::min<int64_t>(nch, (int64_t)sm_count() * 32 / sw);
         sort_scatter_kernel<<<g, 32 * sw, shm * sw, st>>>(m_take, n_take, p_take, pt_keep, s_dev, s_cap, m, nch,
-                                                          hoff, reinterpret_cast<int4*>(sd_rec));
+                                                          chn, hoff, reinterpret_cast<int4*>(sd_rec));
         FBP_LAUNCH_CHECK();
         sort_starts_kernel<<<grid_for(m + 1, 256), 256, 0, st>>>(hoff, m, nch, sd_start);
         FBP_LAUNCH_CHECK();
