@@ -22,7 +22,10 @@ namespace {
 
 constexpr int kMaxCellBits = 16;       // at most 2^16 cells
 constexpr int kPointsPerCell = 64;     // target mean occupancy
-constexpr int kScanThreads = 1024;
+// one CTA of 256 threads scans the cell counts: small enough (about 8K
+// registers) to start beside the tensor-core forward, which leaves about 16K
+// registers of an SM free, instead of waiting for its CTAs to retire
+constexpr int kScanThreads = 256;
 constexpr int kOrderWarps = 8;
 constexpr int kOrderStage = 256;       // segment length staged in shared memory
 
@@ -98,13 +101,14 @@ __global__ void __launch_bounds__(kScanThreads) cell_scan_kernel(const int32_t* 
     if (lane == 31) warp_sums[wid] = v;
     __syncthreads();
     if (wid == 0) {
-        int32_t w = warp_sums[lane];
+        constexpr int NW = kScanThreads / 32;
+        int32_t w = lane < NW ? warp_sums[lane] : 0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int32_t t = __shfl_up_sync(0xffffffffu, w, o);
             if (lane >= o) w += t;
         }
-        warp_sums[lane] = w;
+        if (lane < NW) warp_sums[lane] = w;
     }
     __syncthreads();
     int32_t run = v - s + (wid > 0 ? warp_sums[wid - 1] : 0);  // exclusive prefix of this thread's range
