@@ -848,3 +848,47 @@ def test_stored_layer2_jets_match_recompute(cuda, name, lap, tc, act):
     _, ps0, loss0, gs0, gr0 = run(limit=0)
     assert ps0.zs is None and loss0 == loss
     assert torch.equal(gs0, gr0) and torch.equal(gr0, gr)
+
+
+def test_host_point_order_follows_probe_extent(cuda):
+    """Host batches enter the point set in cell order over the first batch's
+    box, which gives the loss of the drawn order up to FP32 rounding (the same
+    points, summed in another order); a first batch with no extent along a dim
+    turns the ordering off, and the step still runs."""
+    from fbpinns_gb300.trainers import FusedStep
+    from fbpinns_gb300.optim import adam
+    static = decomposition("poisson")
+    layers = random_layers([2, 16, 16, 1], static["m"], seed=3)
+    prob_static = PR.Poisson2D.init_params(n_freq=6, sd=0.1)[0]
+    spec = PR.Poisson2D.fused_spec({"static": {"problem": prob_static}})
+    g = torch.Generator().manual_seed(9)
+    x = torch.rand((1 << 14, 2), generator=g).pin_memory()
+    losses = {}
+    for order in (True, False):
+        eng = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=512, cell_order=order)
+        eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
+        st = FusedStep(eng, spec, adam(1e-3), host_points=1 << 14, x_probe=x, use_graph=False, pipeline=False)
+        assert st.order_host == order
+        st.step(x)
+        torch.cuda.synchronize()
+        st.check()
+        losses[order] = float(st.loss_host.item())
+        if order:  # the point set holds the batch in cell order: the same points, sorted differently
+            a, b = st.ps.x.cpu().numpy(), x.numpy()
+            assert not np.array_equal(a, b)
+            np.testing.assert_array_equal(a[np.lexsort((a[:, 1], a[:, 0]))], b[np.lexsort((b[:, 1], b[:, 0]))])
+    # a slot's pairs are summed by a segmented scan whose shape follows their
+    # lanes in a row of 32 pairs, so another order rounds each point's FP32 sums
+    # differently: equal to FP32 rounding (measured 3.5e-11 relative)
+    assert abs(losses[True] - losses[False]) <= 1e-6 * abs(losses[False])
+    flat = x.clone()
+    flat[:, 1] = 0.5  # no extent along y
+    eng = FBPINNEngine(static, layer_sizes(layers), 3 | _lib.D2_LAPLACIAN, chunk=512)
+    eng.set_theta(pack_layers([tuple(t.float() for t in layer) for layer in layers]))
+    st = FusedStep(eng, spec, adam(1e-3), host_points=1 << 14, x_probe=flat.pin_memory(), use_graph=False,
+                   pipeline=False)
+    assert not st.order_host
+    st.step(flat.pin_memory())
+    torch.cuda.synchronize()
+    st.check()
+    assert np.isfinite(float(st.loss_host.item()))
